@@ -1,0 +1,159 @@
+/*
+ * kore_gpu.h — C ABI of libkoregpu.so, the GB300 (sm_103a) solve path of kore.
+ *
+ * The reference solve path is the script bin/solve.py, which has no in-process API:
+ * it reads A.npz / B.npz (or B_forced.npz), builds PETSc matrices and hands them to
+ * SLEPc (eigenproblem) or a KSP direct solve (forced problem).  Each entry point
+ * below replaces one step of that script; the Python host (kore_gb300.solver and the
+ * drop-in kore_gb300/cli/solve.py) binds them with ctypes.
+ *
+ * Conventions
+ *  - Every function returns an int status (KORE_OK = 0 or a KORE_E* code).
+ *  - Complex numbers are interleaved (re, im) doubles, i.e. numpy complex128.
+ *  - All matrix and vector arguments are HOST pointers unless the name ends in _dev,
+ *    in which case they are device pointers on the plan's device and the call is
+ *    asynchronous on the given CUDA stream (0 = the plan's stream).
+ *  - Vectors are in the ORIGINAL (section-major) unknown order of bin/assemble.py;
+ *    the l-major permutation is internal to the plan.
+ *  - A plan is used by one host thread at a time; distinct plans are independent.
+ */
+#ifndef KORE_GPU_H
+#define KORE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define KORE_OK          0
+#define KORE_EINVAL      1   /* bad argument or a matrix entry outside the block-tridiagonal band */
+#define KORE_ENOMEM      2   /* device allocation failed */
+#define KORE_ECUDA       3   /* a CUDA runtime error */
+#define KORE_ESINGULAR   4   /* zero pivot in a diagonal Schur complement */
+#define KORE_ENOCONV     5   /* eigensolver: nothing converged within maxit restarts */
+#define KORE_ETIMEOUT    6   /* a bounded device wait ran out (error flag set by a kernel) */
+#define KORE_ENOTFACTORED 7  /* solve/eigs before kore_factor */
+#define KORE_ENAN        8   /* NaN or Inf in a solution (bin/solve.py:263-268) */
+
+/* factorisation precisions */
+#define KORE_PREC_FP64   0   /* complex128 block LU, complex128 sweeps */
+#define KORE_PREC_MIXED  1   /* complex64 block LU, FP64 iterative refinement */
+
+/* SLEPc 'which' criteria, same order as bin/solve.py:99-117 */
+#define KORE_WHICH_LM 0
+#define KORE_WHICH_SM 1
+#define KORE_WHICH_LR 2
+#define KORE_WHICH_SR 3
+#define KORE_WHICH_LI 4
+#define KORE_WHICH_SI 5
+#define KORE_WHICH_TM 6
+#define KORE_WHICH_TR 7
+#define KORE_WHICH_TI 8
+
+typedef struct kore_plan kore_plan;
+
+/*
+ * The pencil (A, B) in the CSR form bin/assemble.py writes with np.savez
+ * (bin/assemble.py:591 for B, :1171 for A; loaded by bin/utils.py:1253-1256).
+ * A is complex128, B is float64; B may be absent (b_nnz = 0, pointers NULL) for the
+ * forced problem.  perm[i] is the original index of l-major unknown i; block_sizes
+ * partitions the l-major order into nblocks consecutive diagonal blocks such that
+ * A and B are block tridiagonal.  The plan copies everything it needs; the caller's
+ * arrays may be freed after the call.
+ */
+typedef struct {
+    int64_t n;
+    int64_t a_nnz;
+    const int32_t *a_indptr;    /* n + 1 */
+    const int32_t *a_indices;   /* a_nnz */
+    const double  *a_data;      /* 2 * a_nnz (re, im) */
+    int64_t b_nnz;
+    const int32_t *b_indptr;    /* n + 1, or NULL */
+    const int32_t *b_indices;   /* b_nnz, or NULL */
+    const double  *b_data;      /* b_nnz, or NULL */
+    const int64_t *perm;        /* n */
+    int32_t nblocks;
+    const int32_t *block_sizes; /* nblocks */
+} kore_pencil_desc;
+
+/*
+ * Krylov-Schur options: the fields bin/solve.py sets on SLEPc EPS
+ * (setDimensions(nev) :96, setTolerances(tol, maxit) :97, setWhichEigenpairs :99-117,
+ * setTarget(tau) :119) plus the explicit dimensions SLEPc would choose
+ * (ncv = 0 -> min(n, max(2 nev, nev + 15)), as SLEPc's default).
+ */
+typedef struct {
+    int32_t nev;
+    int32_t ncv;          /* 0 = SLEPc default */
+    double  tol;          /* relative, on the transformed eigenvalue theta */
+    int32_t maxit;        /* restarts */
+    int32_t which;        /* KORE_WHICH_* */
+    double  target_re, target_im;   /* tau; must equal the factorised shift */
+    uint64_t seed;        /* start vector: complex standard normal from this seed */
+    int32_t purify;       /* 1: apply OP once more to each eigenvector (SLEPc default) */
+    double  refine_tol;   /* mixed precision: relative residual of each OP application */
+} kore_eps_opts;
+
+/* Per-call statistics, filled by kore_eigs / kore_solve when the pointer is non-NULL. */
+typedef struct {
+    int32_t nconv;
+    int32_t restarts;          /* Krylov-Schur outer iterations */
+    int32_t op_applies;        /* applications of (A - sigma B)^-1 B */
+    int32_t sweeps;            /* block-tridiagonal forward+back sweeps */
+    int32_t refine_iters_max;  /* mixed precision: worst refinement count of one application */
+    double  solve_resid_max;   /* worst relative residual of one application */
+    double  factor_ms, iterate_ms;
+} kore_stats;
+
+/* Replaces bin/solve.py:40-86 (load_csr + PETSc Mat assembly of A and B). */
+int kore_plan_create(const kore_pencil_desc *desc, int device, kore_plan **plan);
+
+/*
+ * Factorises A - sigma B (block Thomas over the l-major blocks, explicit inverses of
+ * the diagonal Schur complements, Gauss-Jordan with partial pivoting inside each
+ * block).  Replaces the LU that SLEPc's ST sinvert builds inside E.solve()
+ * (bin/solve.py:123) and the KSP preonly+LU factorisation (bin/solve.py:220-227).
+ */
+int kore_factor(kore_plan *plan, double sigma_re, double sigma_im, int precision);
+
+/*
+ * x = (A - sigma B)^-1 b for nrhs right-hand sides stored one after another
+ * (column k at b + 2*n*k).  Replaces K.solve(bvec, x) (bin/solve.py:227).  In mixed
+ * precision the result is refined in FP64 to relative residual <= refine_tol
+ * (refine_tol <= 0 selects 1e-14).
+ */
+int kore_solve(kore_plan *plan, const double *b, double *x, int nrhs, double refine_tol,
+               kore_stats *stats);
+int kore_solve_dev(kore_plan *plan, const void *b_dev, void *x_dev, int nrhs,
+                   double refine_tol, void *stream, kore_stats *stats);
+
+/*
+ * Shift-and-invert Krylov-Schur for A x = lambda B x around the factorised shift.
+ * Replaces E.solve() and the getEigenpair loop (bin/solve.py:123-158).  evals
+ * receives up to ncv complex eigenvalues in SLEPc order (converged first, sorted by
+ * `which`), evecs (may be NULL) up to ncv unit-2-norm eigenvectors in the original
+ * unknown order; *nconv is the number of converged pairs.  Capacity of evals/evecs:
+ * max_pairs pairs.
+ */
+int kore_eigs(kore_plan *plan, const kore_eps_opts *opts, double *evals, double *evecs,
+              int max_pairs, int *nconv, kore_stats *stats);
+
+/* y = A x - lambda B x (FP64, original order, host pointers); residual checks. */
+int kore_residual(kore_plan *plan, double lam_re, double lam_im, const double *x, double *y);
+
+/* Device bytes held by the plan (CSR copies + factors + Krylov workspace). */
+int kore_plan_bytes(const kore_plan *plan, int64_t *bytes);
+
+/* Number of kernels this library launched since load (for launch accounting). */
+int64_t kore_kernel_launches(void);
+
+const char *kore_status_string(int status);
+
+int kore_plan_destroy(kore_plan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KORE_GPU_H */

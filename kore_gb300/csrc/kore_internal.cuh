@@ -1,0 +1,86 @@
+// Internal plan structure and cross-file declarations of libkoregpu.
+#pragma once
+
+#include <vector>
+#include "kore_common.cuh"
+
+// The pencil is stored l-major and padded: block i (of nblocks K) occupies padded
+// slots [i*S, (i+1)*S) where S is the largest block size; slots past the block's
+// own size are identity rows/columns with zero right-hand side.
+struct kore_plan {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+
+    int64_t n = 0;        // unknowns (sizmat)
+    int K = 0;            // blocks
+    int S = 0;            // padded block size
+    int64_t np = 0;       // K*S
+    std::vector<int> bsz, boff;
+
+    // A and B in l-major padded numbering (rows and columns)
+    int *d_arow = nullptr, *d_acol = nullptr, *d_asplit = nullptr;
+    double2 *d_aval = nullptr;
+    int64_t a_nnz = 0;
+    int *d_brow = nullptr, *d_bcol = nullptr;
+    double *d_bval = nullptr;
+    int64_t b_nnz = 0;
+    bool has_b = false;
+    int64_t *d_slot2orig = nullptr;   // np: original index or -1 for a pad slot
+    int *d_bsz = nullptr;             // K
+
+    // factorisation
+    int prec = -1;
+    bool factored = false;
+    double sigma_re = 0, sigma_im = 0;
+    double minf = 0;                  // ||A - sigma B||_inf
+    void *d_sinv = nullptr, *d_W = nullptr, *d_X = nullptr;  // K*S*S each, row-major blocks
+    size_t factor_elt = 0;            // bytes of one complex element of the factors
+    double *d_rscale = nullptr;       // np row equilibration factors
+    void *d_T = nullptr;              // S x 4S Gauss-Jordan work matrix, column-major
+    int *d_piv = nullptr;             // S pivot rows (row chosen for column k)
+    int *d_pidx = nullptr;            // S: panel position of a row or -1
+    int *d_used = nullptr;            // S: row already used as a pivot
+
+    // solve workspace (padded, complex128 unless noted)
+    double2 *d_v[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    void *d_zlo = nullptr, *d_ylo = nullptr;   // sweep work vectors in factor precision
+    double *d_red = nullptr;          // reduction scratch (4096 doubles)
+    double *h_red = nullptr;          // pinned host mirror
+    int *d_err = nullptr;
+    unsigned *d_bar = nullptr;
+
+    // Krylov-Schur workspace
+    double2 *d_V = nullptr;           // np x (ncv+1)
+    double2 *d_Vtmp = nullptr;        // np x (ncv+1)
+    int ks_cap = 0;
+    double2 *d_H = nullptr;           // small dense matrices of the projected problem
+    double2 *d_small = nullptr;
+
+    size_t bytes = 0;
+    int last_refine_iters = 0;
+    double last_resid = 0;
+};
+
+// plan.cu
+int kore_check_device_error(kore_plan *p);
+int kore_alloc(kore_plan *p, void **ptr, size_t bytes);
+
+// factor.cu
+int kore_factor_impl(kore_plan *p, double sre, double sim, int precision);
+
+// sweep.cu
+// x = (A - sigma B)^-1 b on padded l-major complex128 vectors (device), refined in
+// FP64 when the factors are complex64.  Returns the refinement count in *iters.
+int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol, int *iters,
+                       double *resid);
+// y = B x on padded vectors
+int kore_spmv_b(kore_plan *p, const double2 *x, double2 *y);
+// y = A x - lam B x on padded vectors
+int kore_spmv_pencil(kore_plan *p, double lre, double lim, const double2 *x, double2 *y);
+int kore_gather(kore_plan *p, const double2 *orig, double2 *padded);
+int kore_scatter(kore_plan *p, const double2 *padded, double2 *orig);
+
+// eigs.cu
+int kore_eigs_impl(kore_plan *p, const kore_eps_opts *o, double *evals, double *evecs,
+                   int max_pairs, int *nconv, kore_stats *st);

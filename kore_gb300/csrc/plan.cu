@@ -1,0 +1,332 @@
+// Plan creation and the extern "C" entry points of libkoregpu (include/kore_gpu.h).
+//
+// kore_plan_create replaces the matrix loading of bin/solve.py:40-86: it takes the
+// CSR arrays that bin/assemble.py saved (np.savez, loaded by bin/utils.py:1253-1256),
+// applies the l-major permutation, renumbers rows and columns into padded block
+// slots (block i -> [i*S, (i+1)*S)), checks that every entry of A lies in the
+// block-tridiagonal band and every entry of B in a diagonal block, and uploads the
+// result.  The rows keep their entries sorted by column so each row splits into its
+// L (block i-1), D (block i) and U (block i+1) segments.
+#include "kore_internal.cuh"
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <numeric>
+#include <memory>
+#include <cmath>
+#include <vector>
+
+std::atomic<long long> g_kore_launches{0};
+
+int kore_alloc(kore_plan *p, void **ptr, size_t bytes) {
+    *ptr = nullptr;
+    if (bytes == 0) return KORE_OK;
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return (e == cudaErrorMemoryAllocation) ? KORE_ENOMEM : KORE_ECUDA;
+    }
+    p->bytes += bytes;
+    return KORE_OK;
+}
+
+int kore_check_device_error(kore_plan *p) {
+    int h = 0;
+    KORE_CUDA_TRY(cudaMemcpy(&h, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h == 0) return KORE_OK;
+    KORE_CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
+    if (h == KORE_DEVERR_PIVOT) return KORE_ESINGULAR;
+    return KORE_ETIMEOUT;
+}
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+template <typename T>
+int upload(kore_plan *p, T **dst, const std::vector<T> &src) {
+    KORE_TRY(kore_alloc(p, (void **)dst, src.size() * sizeof(T)));
+    if (!src.empty()) KORE_CUDA_TRY(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return KORE_OK;
+}
+
+void free_plan(kore_plan *p) {
+    void *ptrs[] = {p->d_arow, p->d_acol, p->d_asplit, p->d_aval, p->d_brow, p->d_bcol, p->d_bval,
+                    p->d_slot2orig, p->d_bsz, p->d_sinv, p->d_W, p->d_X, p->d_rscale, p->d_T,
+                    p->d_piv, p->d_pidx, p->d_used, p->d_zlo, p->d_ylo, p->d_red, p->d_err, p->d_bar,
+                    p->d_V, p->d_Vtmp, p->d_H, p->d_small};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    for (auto &v : p->d_v)
+        if (v) cudaFree(v);
+    if (p->h_red) cudaFreeHost(p->h_red);
+    if (p->stream) cudaStreamDestroy(p->stream);
+}
+
+// Permute one CSR matrix.  band = 1: blocks i-1..i+1 allowed (A); band = 0: block i only (B).
+template <typename V>
+int permute_csr(const kore_plan *p, const std::vector<int64_t> &orig2slot, const std::vector<int64_t> &slot2orig,
+                const int32_t *indptr, const int32_t *indices, const V *data, int band, std::vector<int> &row,
+                std::vector<int> &col, std::vector<V> &val, std::vector<int> *split) {
+    const int64_t np = p->np, S = p->S;
+    row.assign(np + 1, 0);
+    for (int64_t s = 0; s < np; ++s) {
+        const int64_t o = slot2orig[s];
+        row[s + 1] = row[s] + (o >= 0 ? indptr[o + 1] - indptr[o] : 0);
+    }
+    const int64_t nnz = row[np];
+    col.resize(nnz);
+    val.resize(nnz);
+    if (split) split->assign(2 * np, 0);
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : bad)
+    for (int64_t s = 0; s < np; ++s) {
+        const int64_t o = slot2orig[s];
+        const int64_t blk = s / S;
+        const int b0 = row[s];
+        if (o < 0) {
+            if (split) { (*split)[2 * s] = b0; (*split)[2 * s + 1] = b0; }
+            continue;
+        }
+        const int e0 = indptr[o], e1 = indptr[o + 1];
+        std::vector<std::pair<int64_t, int>> tmp(e1 - e0);
+        for (int e = e0; e < e1; ++e) {
+            const int64_t c = orig2slot[indices[e]];
+            const int64_t cb = c / S;
+            if (cb < blk - band || cb > blk + band) ++bad;
+            tmp[e - e0] = {c, e};
+        }
+        std::sort(tmp.begin(), tmp.end());
+        int d0 = -1, u0 = -1;
+        for (size_t t = 0; t < tmp.size(); ++t) {
+            col[b0 + t] = (int)tmp[t].first;
+            val[b0 + t] = data[tmp[t].second];
+            const int64_t cb = tmp[t].first / S;
+            if (d0 < 0 && cb >= blk) d0 = b0 + (int)t;
+            if (u0 < 0 && cb >= blk + 1) u0 = b0 + (int)t;
+        }
+        const int end = b0 + (int)tmp.size();
+        if (d0 < 0) d0 = end;
+        if (u0 < 0) u0 = end;
+        if (split) { (*split)[2 * s] = d0; (*split)[2 * s + 1] = u0; }
+    }
+    return bad ? KORE_EINVAL : KORE_OK;
+}
+
+int create(const kore_pencil_desc *d, int device, kore_plan **out) {
+    if (!d || !out || d->n <= 0 || d->nblocks <= 0 || !d->block_sizes || !d->perm || !d->a_indptr)
+        return KORE_EINVAL;
+    if (d->a_nnz >= (int64_t)INT32_MAX || d->b_nnz >= (int64_t)INT32_MAX) return KORE_EINVAL;
+    DeviceGuard g(device);
+    auto *p = new kore_plan();
+    std::unique_ptr<kore_plan, void (*)(kore_plan *)> guard(p, [](kore_plan *q) { free_plan(q); delete q; });
+    p->device = device;
+    p->n = d->n;
+    p->K = d->nblocks;
+    p->bsz.assign(d->block_sizes, d->block_sizes + d->nblocks);
+    p->boff.resize(p->K + 1, 0);
+    for (int i = 0; i < p->K; ++i) {
+        if (p->bsz[i] <= 0) return KORE_EINVAL;
+        p->boff[i + 1] = p->boff[i] + p->bsz[i];
+    }
+    if (p->boff[p->K] != p->n) return KORE_EINVAL;
+    p->S = *std::max_element(p->bsz.begin(), p->bsz.end());
+    if (p->S > 1024) return KORE_EINVAL;
+    p->np = (int64_t)p->K * p->S;
+    if (p->np * 8 >= (int64_t)INT32_MAX) return KORE_EINVAL;
+
+    std::vector<int64_t> orig2slot(p->n, -1), slot2orig(p->np, -1);
+    for (int i = 0; i < p->K; ++i)
+        for (int k = 0; k < p->bsz[i]; ++k) {
+            const int64_t q = p->boff[i] + k;
+            const int64_t o = d->perm[q];
+            if (o < 0 || o >= p->n || orig2slot[o] >= 0) return KORE_EINVAL;
+            orig2slot[o] = (int64_t)i * p->S + k;
+            slot2orig[(int64_t)i * p->S + k] = o;
+        }
+
+    KORE_CUDA_TRY(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+    KORE_CUDA_TRY(cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, device));
+
+    {
+        std::vector<int> row, col, split;
+        std::vector<double2> val;
+        const double2 *adata = reinterpret_cast<const double2 *>(d->a_data);
+        KORE_TRY(permute_csr(p, orig2slot, slot2orig, d->a_indptr, d->a_indices, adata, 1, row, col, val, &split));
+        p->a_nnz = (int64_t)col.size();
+        KORE_TRY(upload(p, &p->d_arow, row));
+        KORE_TRY(upload(p, &p->d_acol, col));
+        KORE_TRY(upload(p, &p->d_aval, val));
+        KORE_TRY(upload(p, &p->d_asplit, split));
+    }
+    p->has_b = d->b_nnz > 0 && d->b_indptr && d->b_indices && d->b_data;
+    if (p->has_b) {
+        std::vector<int> row, col;
+        std::vector<double> val;
+        KORE_TRY(permute_csr(p, orig2slot, slot2orig, d->b_indptr, d->b_indices, d->b_data, 0, row, col, val, nullptr));
+        p->b_nnz = (int64_t)col.size();
+        KORE_TRY(upload(p, &p->d_brow, row));
+        KORE_TRY(upload(p, &p->d_bcol, col));
+        KORE_TRY(upload(p, &p->d_bval, val));
+    }
+    KORE_TRY(upload(p, &p->d_slot2orig, slot2orig));
+    KORE_TRY(upload(p, &p->d_bsz, p->bsz));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_rscale, p->np * sizeof(double)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_piv, p->S * sizeof(int)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_pidx, p->S * sizeof(int)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_used, p->S * sizeof(int)));
+    for (auto &v : p->d_v) KORE_TRY(kore_alloc(p, (void **)&v, p->np * sizeof(double2)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_red, 8192 * sizeof(double)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_err, sizeof(int)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_bar, 64));
+    KORE_CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
+    KORE_CUDA_TRY(cudaMemset(p->d_piv, 0, p->S * sizeof(int)));
+    KORE_CUDA_TRY(cudaMemset(p->d_pidx, 0xff, p->S * sizeof(int)));
+    KORE_CUDA_TRY(cudaMemset(p->d_red, 0, 8192 * sizeof(double)));
+    KORE_CUDA_TRY(cudaMallocHost(&p->h_red, 8192 * sizeof(double)));
+    KORE_CUDA_TRY(cudaDeviceSynchronize());
+    *out = guard.release();
+    return KORE_OK;
+}
+
+int solve_dev_impl(kore_plan *p, const double2 *b, double2 *x, int nrhs, double tol, kore_stats *st) {
+    for (int k = 0; k < nrhs; ++k) {
+        KORE_TRY(kore_gather(p, b + (int64_t)k * p->n, p->d_v[0]));
+        int it = 0;
+        double res = 0.0;
+        KORE_TRY(kore_apply_inverse(p, p->d_v[0], p->d_v[1], tol, &it, &res));
+        KORE_TRY(kore_scatter(p, p->d_v[1], x + (int64_t)k * p->n));
+        if (st) {
+            st->sweeps += std::max(it, 1);
+            st->refine_iters_max = std::max(st->refine_iters_max, it);
+            st->solve_resid_max = std::max(st->solve_resid_max, res);
+        }
+    }
+    return KORE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kore_plan_create(const kore_pencil_desc *desc, int device, kore_plan **plan) {
+    if (plan) *plan = nullptr;
+    return create(desc, device, plan);
+}
+
+int kore_factor(kore_plan *plan, double sigma_re, double sigma_im, int precision) {
+    if (!plan) return KORE_EINVAL;
+    DeviceGuard g(plan->device);
+    return kore_factor_impl(plan, sigma_re, sigma_im, precision);
+}
+
+int kore_solve(kore_plan *p, const double *b, double *x, int nrhs, double refine_tol, kore_stats *stats) {
+    if (!p || !b || !x || nrhs <= 0) return KORE_EINVAL;
+    if (!p->factored) return KORE_ENOTFACTORED;
+    DeviceGuard g(p->device);
+    auto t0 = std::chrono::steady_clock::now();
+    if (stats) *stats = kore_stats{};
+    double2 *db = nullptr, *dx = nullptr;
+    const size_t bytes = (size_t)p->n * nrhs * sizeof(double2);
+    KORE_CUDA_TRY(cudaMallocAsync((void **)&db, bytes, p->stream));
+    KORE_CUDA_TRY(cudaMallocAsync((void **)&dx, bytes, p->stream));
+    int s = KORE_OK;
+    if (cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, p->stream) != cudaSuccess) s = KORE_ECUDA;
+    if (s == KORE_OK) s = solve_dev_impl(p, db, dx, nrhs, refine_tol, stats);
+    if (s == KORE_OK && cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, p->stream) != cudaSuccess) s = KORE_ECUDA;
+    cudaFreeAsync(db, p->stream);
+    cudaFreeAsync(dx, p->stream);
+    if (cudaStreamSynchronize(p->stream) != cudaSuccess && s == KORE_OK) s = KORE_ECUDA;
+    if (s == KORE_OK) s = kore_check_device_error(p);
+    if (s == KORE_OK)
+        for (int64_t i = 0; i < 2 * p->n * nrhs; ++i)
+            if (!std::isfinite(x[i])) { s = KORE_ENAN; break; }
+    if (stats) stats->iterate_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return s;
+}
+
+int kore_solve_dev(kore_plan *p, const void *b_dev, void *x_dev, int nrhs, double refine_tol, void *stream,
+                   kore_stats *stats) {
+    if (!p || !b_dev || !x_dev || nrhs <= 0) return KORE_EINVAL;
+    if (!p->factored) return KORE_ENOTFACTORED;
+    DeviceGuard g(p->device);
+    if (stats) *stats = kore_stats{};
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    cudaEvent_t ev;
+    KORE_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    KORE_CUDA_TRY(cudaEventRecord(ev, cs));
+    KORE_CUDA_TRY(cudaStreamWaitEvent(p->stream, ev, 0));
+    int s = solve_dev_impl(p, static_cast<const double2 *>(b_dev), static_cast<double2 *>(x_dev), nrhs, refine_tol, stats);
+    KORE_CUDA_TRY(cudaEventRecord(ev, p->stream));
+    KORE_CUDA_TRY(cudaStreamWaitEvent(cs, ev, 0));
+    cudaEventDestroy(ev);
+    if (s == KORE_OK) s = kore_check_device_error(p);
+    return s;
+}
+
+int kore_eigs(kore_plan *p, const kore_eps_opts *opts, double *evals, double *evecs, int max_pairs, int *nconv,
+              kore_stats *stats) {
+    if (!p || !opts || !evals || !nconv || max_pairs <= 0) return KORE_EINVAL;
+    DeviceGuard g(p->device);
+    *nconv = 0;
+    return kore_eigs_impl(p, opts, evals, evecs, max_pairs, nconv, stats);
+}
+
+int kore_residual(kore_plan *p, double lre, double lim, const double *x, double *y) {
+    if (!p || !x || !y) return KORE_EINVAL;
+    DeviceGuard g(p->device);
+    const size_t bytes = (size_t)p->n * sizeof(double2);
+    KORE_CUDA_TRY(cudaMemcpyAsync(p->d_v[4], x, bytes, cudaMemcpyHostToDevice, p->stream));
+    KORE_TRY(kore_gather(p, p->d_v[4], p->d_v[0]));
+    KORE_TRY(kore_spmv_pencil(p, lre, lim, p->d_v[0], p->d_v[1]));
+    KORE_TRY(kore_scatter(p, p->d_v[1], p->d_v[4]));
+    KORE_CUDA_TRY(cudaMemcpyAsync(y, p->d_v[4], bytes, cudaMemcpyDeviceToHost, p->stream));
+    KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    return KORE_OK;
+}
+
+int kore_plan_bytes(const kore_plan *p, int64_t *bytes) {
+    if (!p || !bytes) return KORE_EINVAL;
+    *bytes = (int64_t)p->bytes;
+    return KORE_OK;
+}
+
+int64_t kore_kernel_launches(void) { return g_kore_launches.load(); }
+
+const char *kore_status_string(int s) {
+    switch (s) {
+        case KORE_OK: return "ok";
+        case KORE_EINVAL: return "invalid argument or matrix outside the block-tridiagonal band";
+        case KORE_ENOMEM: return "device allocation failed";
+        case KORE_ECUDA: return "CUDA runtime error";
+        case KORE_ESINGULAR: return "zero pivot in a diagonal Schur complement";
+        case KORE_ENOCONV: return "no eigenpair converged";
+        case KORE_ETIMEOUT: return "a bounded device wait ran out";
+        case KORE_ENOTFACTORED: return "plan not factorised";
+        case KORE_ENAN: return "NaN or Inf in the solution";
+    }
+    return "unknown status";
+}
+
+int kore_plan_destroy(kore_plan *p) {
+    if (!p) return KORE_OK;
+    DeviceGuard g(p->device);
+    cudaStreamSynchronize(p->stream);
+    free_plan(p);
+    delete p;
+    return KORE_OK;
+}
+
+}  // extern "C"

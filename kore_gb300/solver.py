@@ -1,0 +1,330 @@
+"""Python host of the GB300 solve path: the objects bin/solve.py builds, backed by
+libkoregpu.so.
+
+``bin/solve.py`` drives petsc4py/slepc4py:
+  * ``Mat`` assembled from the CSR in ``A.npz`` / ``B.npz`` (``bin/solve.py:40-86``),
+  * ``SLEPc.EPS`` configured with ``setProblemType(GNHEP)``, ``setDimensions(nev)``,
+    ``setTolerances(tol, maxit)``, ``setWhichEigenpairs``, ``setTarget`` and
+    ``setFromOptions`` (``bin/solve.py:91-120``), then ``solve()`` and ``getEigenpair``
+    (``bin/solve.py:123-158``),
+  * ``PETSc.KSP`` with ``setOperators(A)``, ``setTolerances``, ``setFromOptions``,
+    ``solve(b, x)`` (``bin/solve.py:219-227``).
+``Pencil``, ``EPS`` and ``KSP`` below keep those names and argument meanings; all
+arithmetic runs in the CUDA library (there is no CPU fallback: a missing library
+raises).
+"""
+import ctypes as C
+import time
+
+import numpy as np
+import scipy.sparse as ss
+
+from . import _lib as L
+from .structure import Layout, band_of, layout_from_params
+
+
+def _csr(M, dtype):
+    M = ss.csr_matrix(M)
+    M.sum_duplicates()
+    M.sort_indices()
+    return (L.as_i32(M.indptr), L.as_i32(M.indices), np.ascontiguousarray(M.data, dtype=dtype))
+
+
+class Pencil:
+    """A (complex128) and optionally B (float64) on the device in l-major block form.
+
+    ``layout`` is a :class:`~kore_gb300.structure.Layout` (or the kore parameters to
+    derive one from).  The device copies are owned by the plan; ``close()`` frees them.
+    """
+
+    def __init__(self, A, B=None, layout=None, params=None, device=0):
+        self.lib = L.load()
+        if layout is None:
+            if params is None:
+                raise ValueError("need a layout or the kore parameters")
+            layout = layout_from_params(params)
+        self.layout = layout
+        n = A.shape[0]
+        if n != layout.n:
+            raise ValueError(f"matrix size {n} does not match the layout ({layout.n})")
+        self.n = n
+        self._a = _csr(A, np.complex128)
+        self._b = _csr(B, np.float64) if B is not None else None
+        self._perm = np.ascontiguousarray(layout.perm, dtype=np.int64)
+        self._bs = L.as_i32(layout.block_sizes)
+        d = L.PencilDesc()
+        d.n = n
+        d.a_nnz = len(self._a[1])
+        d.a_indptr = self._a[0].ctypes.data_as(C.POINTER(C.c_int32))
+        d.a_indices = self._a[1].ctypes.data_as(C.POINTER(C.c_int32))
+        d.a_data = self._a[2].view(np.float64).ctypes.data_as(C.POINTER(C.c_double))
+        if self._b is not None:
+            d.b_nnz = len(self._b[1])
+            d.b_indptr = self._b[0].ctypes.data_as(C.POINTER(C.c_int32))
+            d.b_indices = self._b[1].ctypes.data_as(C.POINTER(C.c_int32))
+            d.b_data = self._b[2].ctypes.data_as(C.POINTER(C.c_double))
+        d.perm = self._perm.ctypes.data_as(C.POINTER(C.c_int64))
+        d.nblocks = len(self._bs)
+        d.block_sizes = self._bs.ctypes.data_as(C.POINTER(C.c_int32))
+        self._plan = C.c_void_p()
+        t = time.perf_counter()
+        L.check(self.lib.kore_plan_create(C.byref(d), int(device), C.byref(self._plan)), "kore_plan_create")
+        self.create_s = time.perf_counter() - t
+        self.sigma = None
+        self.precision = None
+        self.factor_s = None
+
+    # -- factor / solve ---------------------------------------------------------------
+    def factor(self, sigma, precision="fp64"):
+        """Factorise A - sigma*B (block Thomas, see csrc/factor.cu)."""
+        sigma = complex(sigma)
+        t = time.perf_counter()
+        L.check(self.lib.kore_factor(self._plan, sigma.real, sigma.imag, L.PREC[precision]), "kore_factor")
+        self.factor_s = time.perf_counter() - t
+        self.sigma, self.precision = sigma, precision
+        return self
+
+    def solve(self, b, refine_tol=0.0, stats=False):
+        """x = (A - sigma B)^-1 b for a vector or the columns of an (n, k) array."""
+        b = np.asarray(b)
+        one = b.ndim == 1
+        bc = L.as_c128(b.reshape(self.n, -1).T)  # (k, n) rows contiguous
+        x = np.empty_like(bc)
+        st = L.Stats()
+        L.check(self.lib.kore_solve(self._plan, L.ptr(bc), L.ptr(x), bc.shape[0], float(refine_tol), C.byref(st)),
+                "kore_solve")
+        out = x[0] if one else np.ascontiguousarray(x.T)
+        return (out, st.as_dict()) if stats else out
+
+    def solve_dev(self, b_ptr, x_ptr, nrhs=1, refine_tol=0.0, stream=None):
+        """Device-pointer form (complex128, original order); ``stream`` is a cudaStream_t value."""
+        st = L.Stats()
+        L.check(self.lib.kore_solve_dev(self._plan, C.c_void_p(b_ptr), C.c_void_p(x_ptr), int(nrhs),
+                                        float(refine_tol), C.c_void_p(stream or 0), C.byref(st)), "kore_solve_dev")
+        return st.as_dict()
+
+    def residual(self, lam, x):
+        """A x - lam B x (FP64 on the device)."""
+        lam = complex(lam)
+        x = L.as_c128(x)
+        y = np.empty_like(x)
+        L.check(self.lib.kore_residual(self._plan, lam.real, lam.imag, L.ptr(x), L.ptr(y)), "kore_residual")
+        return y
+
+    def device_bytes(self):
+        v = C.c_int64()
+        L.check(self.lib.kore_plan_bytes(self._plan, C.byref(v)), "kore_plan_bytes")
+        return int(v.value)
+
+    def close(self):
+        if getattr(self, "_plan", None) and self._plan.value:
+            self.lib.kore_plan_destroy(self._plan)
+            self._plan = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def kernel_launches():
+    return int(L.load().kore_kernel_launches())
+
+
+class EPS:
+    """Shift-and-invert Krylov-Schur eigensolver with the slepc4py EPS call sequence
+    that ``bin/solve.py:91-123`` uses."""
+
+    class ProblemType:
+        GNHEP = "GNHEP"
+
+    class Which:
+        LARGEST_MAGNITUDE = "LM"
+        SMALLEST_MAGNITUDE = "SM"
+        LARGEST_REAL = "LR"
+        SMALLEST_REAL = "SR"
+        LARGEST_IMAGINARY = "LI"
+        SMALLEST_IMAGINARY = "SI"
+        TARGET_MAGNITUDE = "TM"
+        TARGET_REAL = "TR"
+        TARGET_IMAGINARY = "TI"
+
+    def __init__(self):
+        self.pencil = None
+        self.nev, self.ncv = 1, 0
+        self.tol, self.maxit = 1e-8, 100
+        self.which = "LM"
+        self.target = 0j
+        self.st_type = "sinvert"
+        self.precision = "fp64"
+        self.seed = 0
+        self.purify = True
+        self.refine_tol = 0.0
+        self._lam = np.zeros(0, complex)
+        self._X = None
+        self.stats = {}
+        self.its = 0
+
+    def create(self, comm=None):
+        return self
+
+    def setOperators(self, pencil, B=None):
+        if not isinstance(pencil, Pencil):
+            raise TypeError("EPS.setOperators takes a kore_gb300 Pencil holding A and B")
+        self.pencil = pencil
+
+    def setProblemType(self, ptype):
+        if ptype != "GNHEP":
+            raise ValueError("only the generalized non-Hermitian problem (GNHEP) is on the kore path")
+
+    def setDimensions(self, nev=None, ncv=None, mpd=None):
+        if nev is not None:
+            self.nev = int(nev)
+        if ncv is not None:
+            self.ncv = int(ncv)
+
+    def setTolerances(self, tol=None, max_it=None):
+        if tol is not None:
+            self.tol = float(tol)
+        if max_it is not None:
+            self.maxit = int(max_it)
+
+    def setWhichEigenpairs(self, which):
+        if which not in L.WHICH:
+            raise ValueError(f"unknown which {which!r}")
+        self.which = which
+
+    def setTarget(self, tau):
+        self.target = complex(tau)
+
+    def setFromOptions(self, options=None):
+        """Apply PETSc-style options (dict of option -> value, without the dash)."""
+        o = options or {}
+        if "st_type" in o:
+            if o["st_type"] != "sinvert":
+                raise ValueError("only -st_type sinvert is on the kore path")
+        if "eps_nev" in o:
+            self.nev = int(o["eps_nev"])
+        if "eps_ncv" in o:
+            self.ncv = int(o["eps_ncv"])
+        if "eps_tol" in o:
+            self.tol = float(o["eps_tol"])
+        if "eps_max_it" in o:
+            self.maxit = int(o["eps_max_it"])
+        if "eps_purify" in o:
+            self.purify = str(o["eps_purify"]).lower() not in ("0", "false", "no")
+        if "kore_precision" in o:
+            self.precision = o["kore_precision"]
+        if "kore_seed" in o:
+            self.seed = int(o["kore_seed"])
+        if "kore_refine_tol" in o:
+            self.refine_tol = float(o["kore_refine_tol"])
+
+    def getDimensions(self):
+        n = self.pencil.n
+        ncv = self.ncv or min(n, max(2 * self.nev, self.nev + 15))
+        return self.nev, ncv, ncv
+
+    def getTolerances(self):
+        return self.tol, self.maxit
+
+    def getTarget(self):
+        return self.target
+
+    def getType(self):
+        return "krylovschur"
+
+    def solve(self):
+        p = self.pencil
+        if p.sigma != self.target or p.precision != self.precision:
+            p.factor(self.target, self.precision)
+        nev, ncv, _ = self.getDimensions()
+        o = L.EpsOpts(nev=nev, ncv=ncv, tol=self.tol, maxit=self.maxit, which=L.WHICH[self.which],
+                      target_re=self.target.real, target_im=self.target.imag, seed=self.seed,
+                      purify=1 if self.purify else 0, refine_tol=self.refine_tol)
+        ev = np.zeros(ncv, dtype=np.complex128)
+        X = np.zeros((ncv, p.n), dtype=np.complex128)
+        nconv = C.c_int(0)
+        st = L.Stats()
+        t = time.perf_counter()
+        s = p.lib.kore_eigs(p._plan, C.byref(o), L.ptr(ev), L.ptr(X), ncv, C.byref(nconv), C.byref(st))
+        self.solve_s = time.perf_counter() - t
+        self.stats = st.as_dict()
+        self.stats["factor_s"] = p.factor_s
+        if s not in (L.KORE_OK, 5):  # KORE_ENOCONV leaves nconv = 0 (bin/solve.py:192-199)
+            L.check(s, "kore_eigs")
+        k = nconv.value
+        self.its = st.restarts
+        self._lam = ev[:k].copy()
+        self._X = np.ascontiguousarray(X[:k].T)
+        return self
+
+    def getConverged(self):
+        return len(self._lam)
+
+    def getIterationNumber(self):
+        return self.its
+
+    def getEigenpair(self, i, Vr=None, Vi=None):
+        """Eigenvalue i; if ``Vr`` is a numpy array it receives the eigenvector."""
+        if Vr is not None:
+            Vr[...] = self._X[:, i]
+        return complex(self._lam[i])
+
+    def eigenvalues(self):
+        return self._lam.copy()
+
+    def eigenvectors(self):
+        return self._X
+
+
+class KSP:
+    """Direct solve ``-ksp_type preonly -pc_type lu`` (``bin/solve.py:219-227``)."""
+
+    def __init__(self):
+        self.pencil = None
+        self.rtol, self.max_it = 1e-8, 10000
+        self.precision = "fp64"
+        self.refine_tol = 0.0
+        self.stats = {}
+
+    def create(self, comm=None):
+        return self
+
+    def setOperators(self, pencil):
+        if not isinstance(pencil, Pencil):
+            raise TypeError("KSP.setOperators takes a kore_gb300 Pencil holding A")
+        self.pencil = pencil
+
+    def setTolerances(self, rtol=None, max_it=None):
+        if rtol is not None:
+            self.rtol = float(rtol)
+        if max_it is not None:
+            self.max_it = int(max_it)
+
+    def setFromOptions(self, options=None):
+        o = options or {}
+        if o.get("ksp_type", "preonly") != "preonly" or o.get("pc_type", "lu") != "lu":
+            raise ValueError("only -ksp_type preonly -pc_type lu is on the kore path")
+        if "kore_precision" in o:
+            self.precision = o["kore_precision"]
+        if "kore_refine_tol" in o:
+            self.refine_tol = float(o["kore_refine_tol"])
+
+    def solve(self, b, x=None):
+        p = self.pencil
+        if p.sigma != 0j or p.precision != self.precision:
+            p.factor(0.0, self.precision)
+        sol, st = p.solve(b, refine_tol=self.refine_tol, stats=True)
+        self.stats = st
+        if x is not None:
+            x[...] = sol
+            return x
+        return sol

@@ -1,0 +1,137 @@
+#!/usr/bin/env python3
+"""Generate the golden pencil fixtures in ``tests/golden/`` from the reference itself.
+
+For each case this script
+  1. copies the reference's ``bin/`` into a scratch directory,
+  2. writes ``bin/parameters.py`` from a base parameter file plus overrides
+     (the same ``sed`` style edit the reference's own tests and tools use,
+     ``tests/jones2000/find_Rac.py:31``),
+  3. runs the reference's unmodified ``compute_profiles.py`` (magnetic cases),
+     ``submatrices.py`` and ``assemble.py``, the latter under the single-rank
+     ``mpi4py`` stand-in in ``_standin/``,
+  4. stores A, B (or the forcing column) and the derived sizes in
+     ``tests/golden/<case>.npz``.
+
+It needs the reference checkout (default ``/root/reference``, or ``$KORE_REF``) and
+is run by hand; the fixtures it writes are committed so that the tests never read
+the reference at run time.
+
+    python tests/golden/make_fixtures.py [case ...]
+"""
+import json
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.environ.get("KORE_REF", "/root/reference")
+STANDIN = os.path.join(HERE, "_standin")
+
+# case name -> (base parameter file relative to the reference root, overrides, needs profiles)
+CASES = {
+    # the reference's spin-over test, byte-identical parameters (tests/spinover/params.spinover)
+    "spinover": ("tests/spinover/params.spinover", {}, False),
+    # hydrodynamic shell, m=1 symmetric, Ek=1e-4, N=48, lmax=40 (2k unknowns)
+    "shell_m1_ek1e-4": ("bin/parameters.py", {
+        "symm": "1", "Ek": "1e-4", "N": "48", "lmax": "40", "itau": "1.0",
+        "nev": "10", "which_eigenpairs": "'TM'"}, False),
+    # smaller hydrodynamic shell with an m=2 target on the imaginary axis
+    "shell_m2_small": ("bin/parameters.py", {
+        "m": "2", "symm": "1", "Ek": "1e-5", "N": "40", "lmax": "31", "itau": "0.5",
+        "nev": "16", "which_eigenpairs": "'TM'"}, False),
+    # forced problem: m=2 radial boundary forcing (forcing 10), omega = 0.7
+    "forced_m2_f10": ("bin/parameters.py", {
+        "m": "2", "symm": "1", "Ek": "1e-4", "N": "40", "lmax": "31",
+        "forcing": "10", "forcing_frequency": "0.7"}, False),
+    # forced problem: m=2 libration (forcing 7), omega = -1.3
+    "forced_m2_f7": ("bin/parameters.py", {
+        "m": "2", "symm": "1", "Ek": "1e-4", "N": "32", "lmax": "21",
+        "forcing": "7", "forcing_frequency": "-1.3"}, False),
+    # the same m=2 shell as an eigenproblem (forced A = |B|_F (A_eig - i w B_eig))
+    "shell_m2_ek1e-4": ("bin/parameters.py", {
+        "m": "2", "symm": "1", "Ek": "1e-4", "N": "40", "lmax": "31", "itau": "0.5",
+        "nev": "8"}, False),
+    # Jones et al. 2000 onset at the golden critical Rayleigh number (tests/jones2000)
+    "jones2000_rac": ("tests/jones2000/params.jones", {
+        "Ra_gap": "4.66986e6", "nev": "12", "which_eigenpairs": "'TR'"}, False),
+    # Dormy et al. 2004 onset at the golden critical Rayleigh number (tests/dormy2004)
+    "dormy2004_rac": ("tests/dormy2004/params.dormy04", {
+        "Ra_gap": "1.65404e6", "nev": "12", "which_eigenpairs": "'TR'"}, False),
+    # small magneto-Archimedes-Coriolis case: dipole B0, insulating mantle, thermal
+    "mac_dipole_small": ("bin/parameters.py", {
+        "symm": "1", "Ek": "1e-3", "N": "24", "lmax": "16", "itau": "0.1",
+        "magnetic": "1", "thermal": "1", "B0": "'dipole'", "Pm": "1e-3",
+        "Lambda": "0.1", "Ra_gap": "1e5", "nev": "8"}, True),
+    # small quadrupole-field case (l +- 2 coupling through B0)
+    "mac_quadrupole_small": ("bin/parameters.py", {
+        "symm": "1", "Ek": "1e-3", "N": "24", "lmax": "16", "itau": "0.1",
+        "magnetic": "1", "B0": "'Luo_S2'", "Pm": "1e-3", "Lambda": "0.1",
+        "nev": "8"}, True),
+}
+
+DERIVED = ("m symm ricb N lmax hydro magnetic thermal compositional B0 forcing "
+           "forcing_frequency nev tol maxit which_eigenpairs Ek").split()
+
+
+def edit_params(text, overrides):
+    for name, value in overrides.items():
+        pat = re.compile(r"^(\s*)" + re.escape(name) + r"\s*=.*$", re.M)
+        if not pat.search(text):
+            raise KeyError(f"parameter {name} not found")
+        text = pat.sub(lambda mo: f"{mo.group(1)}{name} = {value}", text, count=1)
+    return text
+
+
+def run(cmd, cwd, env=None):
+    r = subprocess.run(cmd, cwd=cwd, env=env, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{' '.join(cmd)} failed:\n{r.stdout[-2000:]}\n{r.stderr[-4000:]}")
+    return r.stdout
+
+
+def make_case(name):
+    base, overrides, profiles = CASES[name]
+    with tempfile.TemporaryDirectory(prefix=f"korefx_{name}_") as tmp:
+        shutil.copytree(os.path.join(REF, "bin"), os.path.join(tmp, "bin"))
+        with open(os.path.join(REF, base)) as f:
+            text = edit_params(f.read(), overrides)
+        with open(os.path.join(tmp, "bin", "parameters.py"), "w") as f:
+            f.write(text)
+        env = dict(os.environ)
+        env["PYTHONPATH"] = STANDIN + os.pathsep + env.get("PYTHONPATH", "")
+        py = sys.executable
+        if profiles:
+            run([py, "bin/compute_profiles.py"], tmp, env)
+        run([py, "bin/submatrices.py", "4"], tmp, env)
+        run([py, "bin/assemble.py"], tmp, env)
+        probe = ("import sys, json; sys.path.insert(0, 'bin'); import parameters as par, utils as ut;"
+                 "d = {k: getattr(par, k) for k in %r};"
+                 "d['tau'] = [float(par.tau.real), float(par.tau.imag)];"
+                 "d.update(N1=int(ut.N1), n=int(ut.n), sizmat=int(ut.sizmat), symmB0=int(ut.symmB0));"
+                 "print(json.dumps(d, default=lambda v: v.item() if hasattr(v, 'item') else str(v)))"
+                 % (DERIVED,))
+        meta = json.loads(run([py, "-c", probe], tmp, env).strip().splitlines()[-1])
+        out = {"meta": np.array(json.dumps(meta))}
+        a = np.load(os.path.join(tmp, "A.npz"))
+        for k in ("data", "indices", "indptr", "shape"):
+            out["A_" + k] = a[k]
+        bname = "B.npz" if meta["forcing"] == 0 else "B_forced.npz"
+        b = np.load(os.path.join(tmp, bname))
+        for k in ("data", "indices", "indptr", "shape"):
+            out["B_" + k] = b[k]
+        dst = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(dst, **out)
+        return name, meta["sizmat"], os.path.getsize(dst)
+
+
+if __name__ == "__main__":
+    names = sys.argv[1:] or list(CASES)
+    from concurrent.futures import ProcessPoolExecutor
+    with ProcessPoolExecutor(max_workers=min(4, len(names))) as ex:
+        for name, sizmat, size in ex.map(make_case, names):
+            print(f"{name}: sizmat={sizmat} file={size/1e6:.2f} MB")
