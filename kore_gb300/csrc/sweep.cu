@@ -338,7 +338,8 @@ int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol, i
             const double den = p->minf * xmax + bmax;
             eta = (den > 0.0) ? rmax / den : 0.0;
             if (!(eta == eta)) return KORE_ENAN;
-            if (eta <= tol || eta > 0.5 * prev) break;
+            // converged, or no longer improving (FP64 residual floor reached)
+            if (eta <= tol || eta > 0.9 * prev) break;
             prev = eta;
             KORE_CUDA_TRY(cudaMemcpyAsync(rn, &rmax, sizeof(double), cudaMemcpyHostToDevice, p->stream));
             KORE_TRY(sweep(p, r, rn, x, 1));
