@@ -1,0 +1,360 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 solve path: converged eigenpairs/s of the shift-and-invert
+Krylov-Schur solve, mixed precision (complex64 block factorisation + FP64 refinement)
+against the plain FP64 GPU path, with p50/p99 per-solve latency.
+
+Workload (default ``--workload shell2``): hydrodynamic inertial modes in a spherical
+shell, ricb=0.35, no-slip, m=2, equatorially symmetric, Ek=1e-7, N=400, lmax=601
+(240,000 complex unknowns, 600 l-blocks of 400), target 0.5i, nev=16, which='TM'.
+The pencil is assembled on the host by kore_gb300.assembly (a restatement of
+bin/assemble.py that reproduces the reference's matrices to ~1e-16).
+
+A step is one complete eigen solve (factorise A - tau B, Krylov-Schur to nev converged
+pairs) with the pencil resident on the device.  ``e2e`` times the same solve through
+the C-ABI with host buffers: plan creation from the host CSR (host->device copy),
+factorisation, eigensolve and the eigenvalues+eigenvectors back to host memory.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (m, symm, Ek, N, lmax, ricb, tau, nev, which)
+    "shell2": (2, 1, 1e-7, 400, 601, 0.35, 0.5j, 16, "TM"),
+    "shell1": (1, 1, 1e-4, 48, 40, 0.35, 1.0j, 10, "TM"),
+    # the same shell with 120 l-blocks: small case for profiler captures
+    "shell2s": (2, 1, 1e-7, 400, 121, 0.35, 0.5j, 16, "TM"),
+}
+
+
+def describe(w):
+    m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[w]
+    return (f"hydro shell ricb={ricb} no-slip m={m} symm={symm} Ek={Ek:g} N={N} lmax={lmax}, "
+            f"target {tau.imag:g}i, nev={nev}, which={which}")
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d["hbm_gbs"], d.get("bf16_tflops"), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def build_pencil(w):
+    from kore_gb300.assembly import hydro_params, hydro_pencil
+    from kore_gb300.structure import layout_from_params
+    m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[w]
+    A, B = hydro_pencil(m, symm, Ek, N, lmax, ricb)
+    lay = layout_from_params(hydro_params(m, symm, Ek, N, lmax, ricb))
+    return A, B, lay
+
+
+def run_eps(p, tau, nev, which, precision, seed, want_vectors=True, tol=1e-15, maxit=50):
+    from kore_gb300 import EPS
+    E = EPS()
+    E.setOperators(p)
+    E.setProblemType(EPS.ProblemType.GNHEP)
+    E.setDimensions(nev)
+    E.setTolerances(tol, maxit)
+    E.setWhichEigenpairs(which)
+    E.setTarget(tau)
+    E.setFromOptions({"st_type": "sinvert", "kore_precision": precision, "kore_seed": seed})
+    p.sigma = None  # every step factorises afresh
+    E.solve()
+    return E
+
+
+def rel_residuals(A, B, lam, X):
+    import scipy.sparse.linalg as ssl
+    na, nb = ssl.norm(A, 1), ssl.norm(B, 1)
+    out = []
+    for j, l in enumerate(lam):
+        x = X[:, j]
+        out.append(np.linalg.norm(A @ x - l * (B @ x)) / ((na + abs(l) * nb) * np.linalg.norm(x)))
+    return np.array(out)
+
+
+def time_arm(p, torch, stream, w, precision, steps, warmup, seed0=1):
+    m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[w]
+    for s in range(warmup):
+        run_eps(p, tau, nev, which, precision, seed0 + s)
+    lat, pairs = [], 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(steps):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        E = run_eps(p, tau, nev, which, precision, seed0 + warmup + s)
+        ev1.record(stream)
+        ev1.synchronize()
+        lat.append(ev0.elapsed_time(ev1))
+        pairs += min(E.getConverged(), nev)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    return E, lat, pairs, wall
+
+
+def reference_arm(args, rank, world):
+    """The reference's CPU solve path restated by the oracle (SuperLU + ARPACK), timed on
+    the host cores on a bounded sample of the workload and scaled to the full one."""
+    if rank != 0:
+        return
+    from kore_gb300.assembly import hydro_pencil
+    from oracle.eps_ref import shift_invert_eigs
+    m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[args.workload]
+    lsample = min(lmax, 41)
+    if (lsample - m + 1) % 2:
+        lsample += 1
+    A, B = hydro_pencil(m, symm, Ek, N, lsample, ricb)
+    kfull = (lmax - m + 1)
+    ksamp = (lsample - m + 1)
+    ts = []
+    for s in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        lam, X = shift_invert_eigs(A, B, tau, nev, which, seed=s)
+        dt = time.perf_counter() - t
+        if s >= args.warmup:
+            ts.append(dt)
+    per = float(np.mean(ts)) * kfull / ksamp
+    value = nev / per
+    cores = os.cpu_count()
+    line = {"metric": "eigenpairs/s (shift-invert Krylov-Schur, nev converged)", "value": value,
+            "unit": "eigenpairs/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic: pencil assembled from the kore parameters",
+            "config": {"workload": describe(args.workload)}, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "eigenpairs/s", "cores": cores, "kind": "port",
+                             "sample": f"scipy SuperLU + ARPACK (restatement of SLEPc/MUMPS solve.py) on the same "
+                                       f"problem with lmax={lsample} ({ksamp} of {kfull} l-blocks), time scaled "
+                                       f"by {kfull}/{ksamp} (factor and sweeps are linear in the block count)"},
+            "e2e": {"value": value, "unit": "eigenpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(args):
+    """Oracle on a bounded sample (about 10-30 s of CPU work)."""
+    from kore_gb300.assembly import hydro_pencil
+    from oracle.eps_ref import shift_invert_eigs
+    m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[args.workload]
+    lsample = min(lmax, 41)
+    if (lsample - m + 1) % 2:
+        lsample += 1
+    A, B = hydro_pencil(m, symm, Ek, N, lsample, ricb)
+    t = time.perf_counter()
+    shift_invert_eigs(A, B, tau, nev, which, seed=0)
+    dt = time.perf_counter() - t
+    kfull, ksamp = lmax - m + 1, lsample - m + 1
+    per = dt * kfull / ksamp
+    return {"value": nev / per, "unit": "eigenpairs/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"scipy SuperLU + ARPACK on lmax={lsample} ({ksamp}/{kfull} l-blocks, {dt:.1f} s), "
+                      f"scaled to the full workload by the block count"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="shell2", choices=sorted(WORKLOADS))
+    ap.add_argument("--fp64-steps", type=int, default=None)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+
+    from kore_gb300 import Pencil, kernel_launches
+    from kore_gb300 import build as kb
+    kb.build()
+    m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[args.workload]
+    A, B, lay = build_pencil(args.workload)
+
+    # ---- device-resident arms (pencil uploaded once, outside the timed region)
+    p = Pencil(A, B, layout=lay, device=local)
+    stream = torch.cuda.ExternalStream(p.stream(), device=torch.device("cuda", local))
+
+    # FP64 plain GPU path
+    fsteps = args.fp64_steps if args.fp64_steps is not None else args.steps
+    lat64, pairs64, stats64 = [], 0, {}
+    if fsteps > 0:
+        E64, lat64, pairs64, wall64 = time_arm(p, torch, stream, args.workload, "fp64", fsteps,
+                                               min(args.warmup, 1))
+        lam64, X64 = E64.eigenvalues(), E64.eigenvectors()
+        stats64 = dict(E64.stats)
+
+    # mixed (chosen form): timed region
+    for s in range(args.warmup):
+        run_eps(p, tau, nev, which, "mixed", 100 + s)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = kernel_launches()
+    p.profile(True)
+    lat, pairs = [], 0
+    with ClockSampler(local) as clocks:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for s in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            E = run_eps(p, tau, nev, which, "mixed", 200 + s)
+            e1.record(stream)
+            e1.synchronize()
+            lat.append(e0.elapsed_time(e1))
+            pairs += min(E.getConverged(), nev)
+        t1.record(stream)
+        t1.synchronize()
+    torch.cuda.synchronize()
+    prof = p.profile(False)
+    launches = kernel_launches() - launches0
+    total_ms = t0.elapsed_time(t1)
+    if dist:
+        tt = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+        pp = torch.tensor([float(pairs)], device="cuda")
+        dist.all_reduce(pp, op=dist.ReduceOp.SUM)
+        pairs = int(pp.item())
+    value = pairs / (total_ms / 1e3)
+    lam, X = E.eigenvalues(), E.eigenvectors()
+    res = rel_residuals(A, B, lam[:nev], X[:, :nev])
+    if lat64:
+        res64 = rel_residuals(A, B, lam64[:nev], X64[:, :nev])
+        dists = np.array([np.min(np.abs(lam64 - l)) / abs(l) for l in lam[:nev]])
+        diff, nmatch = float(dists.max()), int((dists < 1e-10).sum())
+    else:
+        res64, diff, nmatch = np.zeros(1), None, None
+    stats = dict(E.stats)
+    p.close()
+
+    # ---- e2e through the C-ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        ev_ms = []
+        h2d = A.nnz * (16 + 4) + (A.shape[0] + 1) * 4 + B.nnz * (8 + 4) + (B.shape[0] + 1) * 4 + lay.n * 8
+        d2h = 0
+        for s in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            with Pencil(A, B, layout=lay, device=local) as q:
+                Eq = run_eps(q, tau, nev, which, "mixed", 300 + s)
+                lam_q, X_q = Eq.eigenvalues(), Eq.eigenvectors()
+            torch.cuda.synchronize()
+            ev_ms.append((time.perf_counter() - t) * 1e3)
+            d2h = lam_q.nbytes + X_q.nbytes
+        e2e = {"value": nev / (np.mean(ev_ms) / 1e3), "unit": "eigenpairs/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(ev_ms))}
+
+    if rank != 0:
+        return
+    hbm, _, src = peaks()
+    sweep_ms = prof["sweep_ms"] / max(prof["sweeps"], 1)
+    achieved = prof["sweep_bytes"] / (sweep_ms * 1e-3) / 1e9
+    line = {
+        "metric": "eigenpairs/s (shift-invert Krylov-Schur, nev converged, resid<=1e-10), mixed vs FP64 GPU",
+        "value": value, "unit": "eigenpairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 factor + f64 refinement/Krylov", "data": "synthetic: pencil assembled from the kore parameters "
+        "(restatement of bin/assemble.py, matches the reference to 1e-16)",
+        "config": {"workload": describe(args.workload), "n": int(lay.n), "blocks": int(lay.nblocks),
+                   "block": int(lay.block_sizes.max()), "l2": "inputs larger than L2 (factors >= 2.3 GB)",
+                   "parallelism": f"replicas x{world}"},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "fp64": ({"value": pairs64 / (sum(lat64) / 1e3), "unit": "eigenpairs/s",
+                  "p50_ms": float(np.percentile(lat64, 50)), "p99_ms": float(np.percentile(lat64, 99)),
+                  "max_eig_resid": float(res64.max()),
+                  "solver_stats": {k: stats64.get(k) for k in ("restarts", "op_applies", "sweeps")}}
+                 if lat64 else None),
+        "speedup_vs_fp64": (value / (pairs64 / (sum(lat64) / 1e3))) if lat64 else None,
+        "max_eig_resid": float(res.max()), "max_rel_eig_diff_vs_fp64": diff,
+        "eigs_matching_fp64_1e-10": nmatch,
+        "solver_stats": {k: stats.get(k) for k in ("restarts", "op_applies", "sweeps", "refine_iters_max",
+                                                   "solve_resid_max")},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "k_sweep (block-tridiagonal forward+back sweep)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_source": src, "traffic": None, "bytes_per_launch": prof["sweep_bytes"],
+                     "avg_launch_ms": sweep_ms, "launches": prof["sweeps"],
+                     "sweep_share_of_step": prof["sweep_ms"] / total_ms,
+                     "factor_ms_avg": prof["factor_ms"] / max(prof["factors"], 1)},
+        "clocks": clocks.summary(),
+        "e2e": e2e,
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(args)
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

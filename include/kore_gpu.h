@@ -143,6 +143,17 @@ int kore_eigs(kore_plan *plan, const kore_eps_opts *opts, double *evals, double 
 /* y = A x - lambda B x (FP64, original order, host pointers); residual checks. */
 int kore_residual(kore_plan *plan, double lam_re, double lam_im, const double *x, double *y);
 
+/* The CUDA stream (cudaStream_t) every kernel of the plan is launched on. */
+int kore_plan_stream(const kore_plan *plan, void **stream);
+
+/*
+ * Kernel timing with CUDA events on the plan's stream.  enable = 1 starts recording
+ * (and clears the totals), 0 stops.  out (may be NULL) receives 6 doubles:
+ * [sweep kernel ms total, sweep launches, factorisation ms total, factorisations,
+ *  algorithmic bytes of one sweep launch, algorithmic flops of one factorisation].
+ */
+int kore_profile(kore_plan *plan, int enable, double *out);
+
 /* Device bytes held by the plan (CSR copies + factors + Krylov workspace). */
 int kore_plan_bytes(const kore_plan *plan, int64_t *bytes);
 

@@ -21,8 +21,8 @@ WHICH = {"LM": 0, "SM": 1, "LR": 2, "SR": 3, "LI": 4, "SI": 5, "TM": 6, "TR": 7,
 
 # every function include/kore_gpu.h declares
 EXPORTS = ("kore_plan_create", "kore_factor", "kore_solve", "kore_solve_dev", "kore_eigs",
-           "kore_residual", "kore_plan_bytes", "kore_kernel_launches", "kore_status_string",
-           "kore_plan_destroy")
+           "kore_residual", "kore_plan_stream", "kore_profile", "kore_plan_bytes", "kore_kernel_launches",
+           "kore_status_string", "kore_plan_destroy")
 
 
 class KoreError(RuntimeError):
@@ -95,6 +95,8 @@ def _bind(lib):
     lib.kore_solve_dev.argtypes = [P, P, P, C.c_int, C.c_double, P, C.POINTER(Stats)]
     lib.kore_eigs.argtypes = [P, C.POINTER(EpsOpts), P, P, C.c_int, C.POINTER(C.c_int), C.POINTER(Stats)]
     lib.kore_residual.argtypes = [P, C.c_double, C.c_double, P, P]
+    lib.kore_plan_stream.argtypes = [P, C.POINTER(P)]
+    lib.kore_profile.argtypes = [P, C.c_int, P]
     lib.kore_plan_bytes.argtypes = [P, C.POINTER(C.c_int64)]
     lib.kore_kernel_launches.argtypes = []
     lib.kore_kernel_launches.restype = C.c_int64

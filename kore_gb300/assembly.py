@@ -1,0 +1,368 @@
+"""Hydrodynamic pencil of kore, built on the host from the parameters.
+
+Restates, for the hydrodynamic problem in a spherical shell (``ricb > 0``, no
+magnetic field, no buoyancy, Boussinesq), what the reference computes in three
+stages:
+
+* ``bin/submatrices.py``: radial operators ``r^X D^Y`` in the Gegenbauer (ultraspherical)
+  basis.  Chebyshev coefficients of powers of r (``bin/utils.py:251-269``), basis
+  conversion C^(l) -> C^(l+1) (``Slam``, ``bin/utils.py:911-926``), derivatives
+  (``Dlam``, ``bin/utils.py:895-908``) and the multiplication operator by a series in
+  C^(l) (``Mlam``, ``bin/utils.py:962-1051``), assembled as
+  ``G[g][g-Y] * M(S_Y r^X, Y) * D_Y`` with the top ``g`` rows left empty for the tau
+  boundary rows (``bin/submatrices.py:540-590``).  ``g`` = 4 for the poloidal (2curl)
+  equation, 2 for the toroidal (1curl) one.
+* ``bin/operators.py:22-124,141-215``: time-derivative, Coriolis and viscous terms
+  with their degree-dependent coefficients (non-dipole, non-anelastic branches).
+* ``bin/assemble.py``: A = i w u + Coriolis - viscous per degree l, Coriolis coupling
+  l -> l+-1 between the poloidal and toroidal sections, tau rows from
+  ``bc_u_spherical`` (``bin/assemble.py:1188-1296``), B = -u, both divided by ||B||_F
+  for the eigenproblem (``:582-584,1164-1165``); forcing vectors 7, 9 and 10
+  (``:279-427``).
+
+The multiplication operator uses the ultraspherical linearisation coefficients of
+Olver & Townsend (SIAM Review 55, 2013): a closed-form first coefficient followed by
+a three-term ratio recurrence, evaluated here for all (row, column) pairs of the
+band at once.
+"""
+import math
+
+import numpy as np
+import scipy.fft as sfft
+import scipy.sparse as ss
+
+from .structure import ell, radial_size
+
+RCMB = 1.0
+
+
+def ncheb(Ek):
+    """Radial truncation for an Ekman number (``bin/parameters.py:6-16``)."""
+    out = int(17 * Ek ** -0.2) if Ek != 0 else 48
+    return max(48, out + out % 2)
+
+
+def chebco(powr, N, tol, ricb, rcmb=RCMB):
+    """First N Chebyshev coefficients of r^powr on [ricb, rcmb] (``bin/utils.py:251-269``)."""
+    i = np.arange(N)
+    xi = np.cos(np.pi * (i + 0.5) / N)
+    if ricb == 0:
+        ai = (rcmb * xi) ** powr
+    else:
+        ai = (ricb + (rcmb - ricb) * (xi + 1) / 2.0) ** powr
+    out = sfft.dct(ai, type=2) / N
+    out[0] = out[0] / 2.0
+    out[np.abs(out) <= tol] = 0.0
+    return out
+
+
+def conv_mat(lam, N):
+    """C^(lam) -> C^(lam+1) coefficient conversion (bidiagonal, offsets 0 and 2)."""
+    if lam == 0:
+        d0 = 0.5 * np.ones(N)
+        d0[0] = 1.0
+        d2 = -0.5 * np.ones(N - 2)
+    else:
+        t = np.arange(0.0, N)
+        d0 = lam / (lam + t)
+        d2 = -lam / (lam + t[2:])
+    return ss.diags([d0, d2], [0, 2], shape=(N, N), format="csr")
+
+
+def diff_mat(lam, N, ricb, rcmb=RCMB):
+    """d^lam/dr^lam from C^(0) to C^(lam) coefficients."""
+    c1 = (1.0 / rcmb) ** lam if ricb == 0 else (2.0 / (rcmb - ricb)) ** lam
+    c2 = math.factorial(lam - 1) * 2.0 ** (lam - 1)
+    t = lam + np.arange(0, N - lam, dtype=float)
+    return c1 * c2 * ss.diags(t, lam, shape=(N, N), format="csr")
+
+
+def _lin_coeff_first(s, lam, j, k):
+    """Closed form of the first linearisation coefficient c_s^lam(j, k) (vectorised)."""
+    s = np.asarray(s, dtype=np.int64)
+    j = np.asarray(j, dtype=np.int64)
+    k = np.asarray(k, dtype=np.int64)
+    p1 = np.ones(s.shape)
+    p3 = np.ones(s.shape)
+    smax = int(s.max()) if s.size else 0
+    for t in range(smax):
+        on = t < s
+        p1 = np.where(on, p1 * (lam + t) / float(1 + t), p1)
+        p3 = np.where(on, p3 * (2 * lam + j + k - 2 * s + t) / (lam + j + k - 2 * s + t), p3)
+    p2 = np.ones(s.shape)
+    p4 = np.ones(s.shape)
+    js = j - s
+    jmax = int(js.max()) if js.size else 0
+    for t in range(jmax):
+        on = t < js
+        p2 = np.where(on, p2 * (lam + t) / float(1 + t), p2)
+        p4 = np.where(on, p4 * (k - s + 1 + t) / (k - s + lam + t), p4)
+    return p1 * p2 * p3 * p4 * (j + k + lam - 2.0 * s) / (j + k + lam - s)
+
+
+def mult_mat(a0, lam):
+    """Multiplication by the C^(lam) series a0, as an operator on C^(lam) coefficients
+    (no parity reduction: the shell case)."""
+    a0 = np.asarray(a0, dtype=float)
+    N = a0.size
+    if not np.any(a0):
+        return ss.csr_matrix((N, N))
+    if lam == 0:
+        a2 = a0.copy()
+        a2[0] *= 2.0
+        i = np.arange(N)
+        T = a2[np.abs(i[:, None] - i[None, :])]
+        Hk = i[:, None] + i[None, :]
+        H = np.where(Hk < N, a2[np.minimum(Hk, N - 1)], 0.0)
+        H[0, :] = 0.0
+        return ss.csr_matrix(0.5 * (T + H))
+    bw = int(np.nonzero(a0)[0].max())
+    a1 = np.zeros(2 * N)
+    a1[:N] = a0
+    rows, cols = [], []
+    for j in range(N):
+        k1, k2 = max(0, j - bw - 1), min(N, j + bw + 2)
+        for k in range(k1, k2):
+            rows.append(j)
+            cols.append(k)
+    rows = np.array(rows)
+    cols = np.array(cols)
+    # pair (j, k): sum over s = s0..k of a1[2s + j - k] * c_s, with c the recurrence
+    # started at s0 = max(0, k - j) for the index pair (k, |j - k|)
+    s0 = np.maximum(0, cols - rows)
+    jj = cols.copy()
+    kk = np.abs(rows - cols)
+    c = _lin_coeff_first(s0, lam, jj, kk)
+    nsteps = cols - s0 + 1
+    acc = a1[2 * s0 + rows - cols] * c
+    s = s0.astype(float)
+    kcur = kk.astype(float)
+    jf = jj.astype(float)
+    for step in range(1, int(nsteps.max()) if nsteps.size else 0):
+        on = step < nsteps
+        t1 = (jf + kcur + lam - s) * (lam + s) * (jf - s) * (2 * lam + jf + kcur - s) * (kcur - s + lam)
+        t2 = (jf + kcur + lam - s + 1) * (s + 1) * (lam + jf - s - 1) * (lam + jf + kcur - s) * (kcur - s + 1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            cn = c * t1 / t2
+        c = np.where(on, cn, c)
+        s = np.where(on, s + 1, s)
+        kcur = np.where(on, kcur + 2, kcur)
+        idx = np.where(on, (2 * s + rows - cols).astype(np.int64), 0)
+        acc = acc + np.where(on, a1[idx] * c, 0.0)
+    M = ss.csr_matrix((acc, (rows, cols)), shape=(N, N))
+    M.eliminate_zeros()
+    return M
+
+
+class RadialOperators:
+    """The r^X D^Y operators of the two hydrodynamic sections for one (N, ricb)."""
+
+    def __init__(self, N, ricb, tol=1e-9):
+        self.N = N
+        self.ricb = ricb
+        rp = [chebco(x, N, tol, ricb) for x in range(7)]
+        S = [conv_mat(l, N) for l in range(4)]
+        D = [None] + [diff_mat(l, N, ricb) for l in range(1, 5)]
+        ident = ss.identity(N, format="csr")
+        Sto = [ident, S[0], S[1] @ S[0], S[2] @ S[1] @ S[0], S[3] @ S[2] @ S[1] @ S[0]]
+        G4 = [ident, S[3], S[3] @ S[2], S[3] @ S[2] @ S[1], S[3] @ S[2] @ S[1] @ S[0]]
+        G2 = [ident, S[1], S[1] @ S[0]]
+        self._rp, self._Sto, self._D, self._G = rp, Sto, D, {4: G4, 2: G2}
+        self._cache = {}
+
+    def op(self, rx, dx, section):
+        """Operator ``r<rx>_D<dx>_<section>`` with the tau rows emptied."""
+        key = (rx, dx, section)
+        if key in self._cache:
+            return self._cache[key]
+        g = 4 if section == "u" else 2
+        a = self._Sto[dx] @ self._rp[rx]
+        M = self._G[g][g - dx] @ mult_mat(a, dx)
+        if dx > 0:
+            M = M @ self._D[dx]
+        M = ss.csr_matrix(M)
+        M = ss.vstack([ss.csr_matrix((g, self.N)), M[:-g, :]], format="csr")
+        self._cache[key] = M
+        return M
+
+
+def boundary_values(x, N, nder, ricb, rcmb=RCMB):
+    """T_k and its first nder r-derivatives at x = +-1 (``bin/bc_variables.py:8-28``)."""
+    ric = -rcmb if ricb == 0 else ricb
+    out = np.zeros((N, nder + 1))
+    for k in range(N):
+        out[k, 0] = x ** k
+        t = 1.0
+        for i in range(nder):
+            t = t * (k ** 2 - i ** 2) / (2 * i + 1)
+            out[k, i + 1] = x ** (k + i + 1) * t * (2 / (rcmb - ric)) ** (i + 1)
+    return out
+
+
+def hydro_pencil(m, symm, Ek, N, lmax, ricb=0.35, bci=1, bco=1, forcing=0, forcing_frequency=0.0,
+                 forcing_amplitude_cmb=1.0, forcing_amplitude_icb=0.0, Gaspard=1.0, ViscosD=None):
+    """(A, B) as bin/assemble.py writes them for the hydrodynamic shell problem.
+
+    forcing == 0: eigenproblem, B is the (sizmat x sizmat) float64 matrix, A and B
+    divided by ||B||_F.  forcing in (7, 9, 10): forced problem, A = i w u + Coriolis -
+    viscous (unnormalised) and B is the (sizmat x 1) forcing column.
+    """
+    if ricb <= 0:
+        raise ValueError("only the spherical shell (ricb > 0) is assembled here")
+    if (lmax - m + 1) % 2:
+        raise ValueError("lmax - m + 1 must be even")
+    visc = Ek if ViscosD is None else ViscosD
+    N1 = radial_size(N, ricb)
+    nb = (lmax - m + 1) // 2
+    lp, lt = ell(m, lmax, symm)
+    wf = forcing_frequency if forcing else 0.0
+    R = RadialOperators(N, ricb)
+    op = R.op
+    lp_f = lp.astype(float)
+    lt_f = lt.astype(float)
+    Lp = lp_f * (lp_f + 1)
+    Lt = lt_f * (lt_f + 1)
+
+    def kdiag(coef, M):
+        return ss.kron(ss.diags(coef), M, format="csr")
+
+    # --- diagonal blocks: poloidal (section u) and toroidal (section v)
+    uu = [(Lp * Lp, op(2, 0, "u")), (-2 * Lp, op(3, 1, "u")), (-Lp, op(4, 2, "u"))]            # u(l,'u')
+    cu = [(-Lp * 2 * m, op(2, 0, "u")), (2 * 2 * m * np.ones(nb), op(3, 1, "u")),
+          (2 * m * np.ones(nb), op(4, 2, "u"))]                                                # /(1j) coriolis
+    vu = [(-Lp * Lp * (lp_f + 2) * (lp_f - 1), op(0, 0, "u")), (2 * Lp * Lp, op(2, 2, "u")),
+          (-4 * Lp, op(3, 3, "u")), (-Lp, op(4, 4, "u"))]                                      # viscous
+    uv = [(Lt, op(2, 0, "v"))]
+    cv = [(-2 * m * np.ones(nb), op(2, 0, "v"))]
+    vv = [(-Lt * Lt, op(0, 0, "v")), (2 * Lt, op(1, 1, "v")), (Lt, op(2, 2, "v"))]
+
+    def sumk(terms, scale=1.0):
+        out = None
+        for c, M in terms:
+            t = kdiag(scale * c, M)
+            out = t if out is None else out + t
+        return out
+
+    u_p = sumk(uu)
+    u_t = sumk(uv)
+    App = (1j * wf) * u_p + (1j * Gaspard) * sumk(cu) - visc * sumk(vu)
+    Att = (1j * wf) * u_t + (1j * Gaspard) * sumk(cv) - visc * sumk(vv)
+
+    # --- Coriolis coupling l <-> l+-1 between the sections
+    def cpair(l, sgn):
+        if sgn < 0:
+            return (l ** 2 - 1) * np.sqrt(l ** 2 - m ** 2) / (2 * l - 1.0)
+        return l * (l + 2.0) * np.sqrt((l + m + 1.0) * (l - m + 1)) / (2.0 * l + 3.0)
+
+    def coupling(lrow, lcol, sec, terms):
+        rows, cols, c_by_term = [], [], [[] for _ in terms]
+        for k, l in enumerate(lrow):
+            for sgn in (-1, 1):
+                w = np.nonzero(lcol == l + sgn)[0]
+                if w.size == 0:
+                    continue
+                rows.append(k)
+                cols.append(int(w[0]))
+                C = cpair(float(l), sgn)
+                for ti, f in enumerate(terms):
+                    c_by_term[ti].append(2 * C * f(float(l), sgn))
+        out = None
+        for ti, (_, M) in enumerate(terms_ops(sec)):
+            P = ss.csr_matrix((np.array(c_by_term[ti]), (rows, cols)), shape=(len(lrow), len(lcol)))
+            t = ss.kron(P, M, format="csr")
+            out = t if out is None else out + t
+        return Gaspard * out
+
+    def terms_ops(sec):
+        if sec == "u":
+            return [(None, op(3, 0, "u")), (None, op(4, 1, "u"))]
+        return [(None, op(1, 0, "v")), (None, op(2, 1, "v"))]
+
+    # section u row l, utor column l-1: 2C((l-1) r3D0 - r4D1); l+1: 2C(-(l+2) r3D0 - r4D1)
+    fu = [lambda l, s: (l - 1) if s < 0 else -(l + 2), lambda l, s: -1.0]
+    Apt = coupling(lp, lt, "u", fu)
+    Atp = coupling(lt, lp, "v", fu)
+
+    # --- tau rows (bc_u_spherical, no-slip / stress-free, ricb > 0)
+    Tb = boundary_values(1, N, 5, ricb)
+    Ta = boundary_values(-1, N, 4, ricb)
+
+    def bc_rows_u(l):
+        L = l * (l + 1)
+        rows = np.zeros((4, N1), dtype=complex)
+        if bco == 0:
+            rows[0] = Tb[:, 0]
+            rows[1] = (Tb[:, 2] - (2 - L) * Tb[:, 0] / RCMB ** 2) if forcing == 9 else RCMB * Tb[:, 2]
+        else:
+            rows[0] = Tb[:, 0]
+            rows[1] = (Tb[:, 1] + Tb[:, 0]) if forcing == 9 else Tb[:, 1]
+        if bci == 0:
+            rows[2] = Ta[:, 0]
+            rows[3] = ricb * Ta[:, 2]
+        else:
+            rows[2] = Ta[:, 0]
+            rows[3] = Ta[:, 1]
+        return rows
+
+    def bc_rows_v():
+        rows = np.zeros((2, N1), dtype=complex)
+        rows[0] = (-RCMB * Tb[:, 1] + Tb[:, 0]) if bco == 0 else Tb[:, 0]
+        rows[1] = (-ricb * Ta[:, 1] + Ta[:, 0]) if bci == 0 else Ta[:, 0]
+        return rows
+
+    def bc_block(rows_list, nrow):
+        data, ri, ci = [], [], []
+        for k, rows in enumerate(rows_list):
+            for q in range(nrow):
+                nz = np.nonzero(rows[q])[0]
+                data.append(rows[q][nz])
+                ri.append(np.full(nz.size, k * N1 + q))
+                ci.append(k * N1 + nz)
+        return ss.csr_matrix((np.concatenate(data), (np.concatenate(ri), np.concatenate(ci))),
+                             shape=(len(rows_list) * N1, len(rows_list) * N1))
+
+    BCp = bc_block([bc_rows_u(float(l)) for l in lp], 4)
+    BCt = bc_block([bc_rows_v() for _ in lt], 2)
+    A = ss.bmat([[App + BCp, Apt], [Atp, Att + BCt]], format="csr").astype(np.complex128)
+    A.eliminate_zeros()
+    n = 2 * nb * N1
+    if forcing == 0:
+        B = ss.bmat([[-u_p, None], [None, -u_t]], format="csr").astype(np.float64)
+        B.eliminate_zeros()
+        bnorm = ss.linalg.norm(B)
+        return (A / bnorm).tocsr(), (B / bnorm).tocsr()
+    # forcing column (bin/assemble.py:279-427)
+    if forcing == 10:
+        if symm != 1:
+            raise ValueError("forcing 10 needs symm = 1")
+        l = m
+        L = l * (l + 1)
+        pos = N1 * int(np.nonzero(lp == l)[0][0])
+        vals = np.array([1.0 / L, 0.0])
+    elif forcing == 9:
+        if not (symm == 1 and m == 2 and bci == 1):
+            raise ValueError("forcing 9 needs symm = 1, m = 2, bci = 1")
+        L = 6
+        pos = N1 * int(np.nonzero(lp == 2)[0][0])
+        vals = np.array([forcing_amplitude_cmb * RCMB / L, forcing_amplitude_icb * ricb / L])
+    elif forcing == 7:
+        if not (m == 2 and symm == 1 and bci == 1 and bco == 1):
+            raise ValueError("forcing 7 is coded here for m = 2, symm = 1, no-slip")
+        L = 6
+        pos = N1 * int(np.nonzero(lp == 2)[0][0])
+        vals = np.array([-forcing_frequency / L * forcing_amplitude_cmb,
+                         -forcing_frequency / L * forcing_amplitude_icb * ricb ** 2])
+    else:
+        raise ValueError(f"forcing {forcing} is not assembled here")
+    rows = np.arange(pos, pos + 2)
+    keep = vals != 0
+    b = ss.csr_matrix((vals[keep].astype(complex), (rows[keep], np.zeros(keep.sum(), int))), shape=(n, 1))
+    return A, b
+
+
+def hydro_params(m, symm, Ek, N, lmax, ricb=0.35, **kw):
+    """The parameter mapping structure.layout_from_params expects for hydro_pencil."""
+    d = dict(m=m, symm=symm, Ek=Ek, N=N, lmax=lmax, ricb=ricb, hydro=1, magnetic=0, thermal=0,
+             compositional=0, B0="axial")
+    d.update(kw)
+    return d

@@ -348,8 +348,10 @@ int kore_factor_impl(kore_plan *p, double sre, double sim, int precision) {
                                            p->has_b ? 1 : 0, std::hypot(sre, sim), p->d_rscale, p->d_red);
     KORE_LAUNCHED(1);
     KORE_CUDA_TRY(cudaMemcpyAsync(p->h_red, p->d_red, grid * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 1, true));
     int s = (precision == KORE_PREC_FP64) ? factor_dispatch<double2>(p) : factor_dispatch<float2>(p);
     if (s != KORE_OK) return s;
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 1, false));
     KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
     double mx = 0.0;
     for (unsigned b = 0; b < grid; ++b) mx = std::max(mx, p->h_red[b]);

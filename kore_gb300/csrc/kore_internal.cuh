@@ -60,7 +60,19 @@ struct kore_plan {
     size_t bytes = 0;
     int last_refine_iters = 0;
     double last_resid = 0;
+
+    // kernel timing (kore_profile)
+    bool prof = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<std::pair<int, size_t>> ev_marks;   // (kind 0 = sweep, 1 = factor, index of start event)
+    double prof_ms[2] = {0, 0};
+    long long prof_n[2] = {0, 0};
 };
+
+// record a start (begin = true) or stop event of a timed region of `kind`
+int kore_prof_mark(kore_plan *p, int kind, bool begin);
+int kore_prof_collect(kore_plan *p);
 
 // plan.cu
 int kore_check_device_error(kore_plan *p);

@@ -40,6 +40,33 @@ int kore_check_device_error(kore_plan *p) {
     return KORE_ETIMEOUT;
 }
 
+int kore_prof_mark(kore_plan *p, int kind, bool begin) {
+    if (p->ev_used == p->ev_pool.size()) {
+        cudaEvent_t e;
+        KORE_CUDA_TRY(cudaEventCreate(&e));
+        p->ev_pool.push_back(e);
+    }
+    const size_t idx = p->ev_used++;
+    KORE_CUDA_TRY(cudaEventRecord(p->ev_pool[idx], p->stream));
+    if (begin) p->ev_marks.push_back({kind, idx});
+    return KORE_OK;
+}
+
+// Sum the elapsed times of all recorded (start, stop) pairs and recycle the events.
+int kore_prof_collect(kore_plan *p) {
+    KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    for (const auto &m : p->ev_marks) {
+        if (m.second + 1 >= p->ev_used) continue;
+        float ms = 0.f;
+        KORE_CUDA_TRY(cudaEventElapsedTime(&ms, p->ev_pool[m.second], p->ev_pool[m.second + 1]));
+        p->prof_ms[m.first] += ms;
+        p->prof_n[m.first] += 1;
+    }
+    p->ev_marks.clear();
+    p->ev_used = 0;
+    return KORE_OK;
+}
+
 namespace {
 
 struct DeviceGuard {
@@ -63,6 +90,8 @@ int upload(kore_plan *p, T **dst, const std::vector<T> &src) {
 }
 
 void free_plan(kore_plan *p) {
+    for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
+    p->ev_pool.clear();
     void *ptrs[] = {p->d_arow, p->d_acol, p->d_asplit, p->d_aval, p->d_brow, p->d_bcol, p->d_bval,
                     p->d_slot2orig, p->d_bsz, p->d_sinv, p->d_W, p->d_X, p->d_rscale, p->d_T,
                     p->d_piv, p->d_pidx, p->d_used, p->d_zlo, p->d_ylo, p->d_red, p->d_err, p->d_bar,
@@ -294,6 +323,38 @@ int kore_residual(kore_plan *p, double lre, double lim, const double *x, double 
     KORE_TRY(kore_scatter(p, p->d_v[1], p->d_v[4]));
     KORE_CUDA_TRY(cudaMemcpyAsync(y, p->d_v[4], bytes, cudaMemcpyDeviceToHost, p->stream));
     KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    return KORE_OK;
+}
+
+int kore_plan_stream(const kore_plan *p, void **stream) {
+    if (!p || !stream) return KORE_EINVAL;
+    *stream = (void *)p->stream;
+    return KORE_OK;
+}
+
+int kore_profile(kore_plan *p, int enable, double *out) {
+    if (!p) return KORE_EINVAL;
+    DeviceGuard g(p->device);
+    KORE_TRY(kore_prof_collect(p));
+    if (out) {
+        const double e = p->factor_elt ? (double)p->factor_elt : 16.0;
+        const double S = p->S, K = p->K, np = (double)p->np;
+        out[0] = p->prof_ms[0];
+        out[1] = (double)p->prof_n[0];
+        out[2] = p->prof_ms[1];
+        out[3] = (double)p->prof_n[1];
+        // one sweep reads Sinv, W, X (K S^2 each), the right-hand side (16 B) and row
+        // scales (8 B), writes/reads z and y in factor precision and writes x (16 B)
+        out[4] = 3.0 * K * S * S * e + np * (16.0 + 8.0 + 16.0) + 4.0 * np * e;
+        // Gauss-Jordan on [S_i | U_i | L_i | I]: sum over panels of the trailing update
+        // 8 * S * nb * (4S - k0 - nb) real flops, i.e. ~8 * S * (4 S^2 - S^2 / 2) per block
+        out[5] = K * 8.0 * S * (4.0 * S * S - 0.5 * S * S);
+    }
+    if (enable) {
+        p->prof_ms[0] = p->prof_ms[1] = 0.0;
+        p->prof_n[0] = p->prof_n[1] = 0;
+    }
+    p->prof = enable != 0;
     return KORE_OK;
 }
 

@@ -252,8 +252,11 @@ int launch_sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x
 }
 
 int sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int accumulate) {
-    return (p->prec == KORE_PREC_FP64) ? launch_sweep<double2>(p, b, bnorm, x, accumulate)
-                                       : launch_sweep<float2>(p, b, bnorm, x, accumulate);
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 0, true));
+    const int s = (p->prec == KORE_PREC_FP64) ? launch_sweep<double2>(p, b, bnorm, x, accumulate)
+                                              : launch_sweep<float2>(p, b, bnorm, x, accumulate);
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 0, false));
+    return s;
 }
 
 // ||v||_inf of a padded vector into d_red[slot] (device)

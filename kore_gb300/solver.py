@@ -111,6 +111,20 @@ class Pencil:
         L.check(self.lib.kore_residual(self._plan, lam.real, lam.imag, L.ptr(x), L.ptr(y)), "kore_residual")
         return y
 
+    def stream(self):
+        """cudaStream_t (as an int) the plan launches its kernels on."""
+        s = C.c_void_p()
+        L.check(self.lib.kore_plan_stream(self._plan, C.byref(s)), "kore_plan_stream")
+        return int(s.value or 0)
+
+    def profile(self, enable):
+        """Start (True) / stop (False) CUDA-event timing of the sweep and factorisation
+        kernels; returns the totals recorded so far."""
+        out = np.zeros(6)
+        L.check(self.lib.kore_profile(self._plan, 1 if enable else 0, L.ptr(out)), "kore_profile")
+        return {"sweep_ms": out[0], "sweeps": int(out[1]), "factor_ms": out[2], "factors": int(out[3]),
+                "sweep_bytes": out[4], "factor_flops": out[5]}
+
     def device_bytes(self):
         v = C.c_int64()
         L.check(self.lib.kore_plan_bytes(self._plan, C.byref(v)), "kore_plan_bytes")
