@@ -4,6 +4,17 @@
 #include <vector>
 #include "kore_common.cuh"
 
+// One level of the block cyclic reduction.  Couplings of levels >= 1 are dense S x S
+// blocks in kore_plan::d_LU: L of position q at lu_L + q, U at lu_U + q (block units).
+struct BcrLevel {
+    int Kl;          // active blocks
+    int stride;      // original index of position q is q * stride
+    int nodd;        // eliminated at this level: positions 1, 3, ...
+    int neven;       // surviving: positions 0, 2, ...
+    int64_t lu_L, lu_U;        // this level's couplings (-1 at level 0: they come from the CSR)
+    int64_t lu_nL, lu_nU;      // next level's couplings (-1 when the next level is the top)
+};
+
 // The pencil is stored l-major and padded: block i (of nblocks K) occupies padded
 // slots [i*S, (i+1)*S) where S is the largest block size; slots past the block's
 // own size are identity rows/columns with zero right-hand side.
@@ -29,22 +40,30 @@ struct kore_plan {
     int64_t *d_slot2orig = nullptr;   // np: original index or -1 for a pad slot
     int *d_bsz = nullptr;             // K
 
-    // factorisation
+    // factorisation: block cyclic reduction (factor.cu).  Level l has lev[l].Kl active
+    // blocks i = q * 2^l; the odd positions are eliminated, the even ones carry on.
     int prec = -1;
     bool factored = false;
     double sigma_re = 0, sigma_im = 0;
     double minf = 0;                  // ||A - sigma B||_inf
-    void *d_sinv = nullptr, *d_W = nullptr, *d_X = nullptr;  // K*S*S each, row-major blocks
     size_t factor_elt = 0;            // bytes of one complex element of the factors
+    int nlev = 0;                     // reduction levels (the top block is solved after them)
+    std::vector<struct BcrLevel> lev; // host copy of the level table
+    struct BcrLevel *d_lev = nullptr; // device copy
+    int64_t lu_mats = 0;              // dense coupling matrices of levels >= 1
+    int nodd_max = 1;                 // largest number of blocks eliminated at one level
+    // S x S column-major blocks, indexed by original block number
+    void *d_Dinv = nullptr, *d_Gm = nullptr, *d_Hm = nullptr, *d_Dw = nullptr;
+    void *d_LU = nullptr;             // lu_mats blocks
+    void *d_T = nullptr;              // nodd_max x (S x 4S) Gauss-Jordan work, column-major
     double *d_rscale = nullptr;       // np row equilibration factors
-    void *d_T = nullptr;              // S x 4S Gauss-Jordan work matrix, column-major
-    int *d_piv = nullptr;             // S pivot rows (row chosen for column k)
-    int *d_pidx = nullptr;            // S: panel position of a row or -1
-    int *d_used = nullptr;            // S: row already used as a pivot
+    int *d_piv = nullptr;             // nodd_max x S: pivot row chosen for column k
+    int *d_pidx = nullptr;            // nodd_max x S: position of a row in the current panel or -1
+    int *d_used = nullptr;            // nodd_max x S: row already used as a pivot
 
     // solve workspace (padded, complex128 unless noted)
     double2 *d_v[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    void *d_zlo = nullptr, *d_ylo = nullptr;   // sweep work vectors in factor precision
+    void *d_zlo = nullptr, *d_xlo = nullptr, *d_flo = nullptr;   // sweep vectors in factor precision
     double *d_red = nullptr;          // reduction scratch (4096 doubles)
     double *h_red = nullptr;          // pinned host mirror
     int *d_err = nullptr;
@@ -54,10 +73,10 @@ struct kore_plan {
     double2 *d_V = nullptr;           // np x (ncv+1)
     double2 *d_Vtmp = nullptr;        // np x (ncv+1)
     int ks_cap = 0;
-    double2 *d_H = nullptr;           // small dense matrices of the projected problem
     double2 *d_small = nullptr;
 
     size_t bytes = 0;
+    int sweep_occ[2] = {0, 0};        // co-resident sweep CTAs per SM (complex64, complex128)
     int last_refine_iters = 0;
     double last_resid = 0;
 
@@ -79,6 +98,7 @@ int kore_check_device_error(kore_plan *p);
 int kore_alloc(kore_plan *p, void **ptr, size_t bytes);
 
 // factor.cu
+void kore_build_levels(kore_plan *p);
 int kore_factor_impl(kore_plan *p, double sre, double sim, int precision);
 
 // sweep.cu

@@ -93,9 +93,9 @@ void free_plan(kore_plan *p) {
     for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
     p->ev_pool.clear();
     void *ptrs[] = {p->d_arow, p->d_acol, p->d_asplit, p->d_aval, p->d_brow, p->d_bcol, p->d_bval,
-                    p->d_slot2orig, p->d_bsz, p->d_sinv, p->d_W, p->d_X, p->d_rscale, p->d_T,
-                    p->d_piv, p->d_pidx, p->d_used, p->d_zlo, p->d_ylo, p->d_red, p->d_err, p->d_bar,
-                    p->d_V, p->d_Vtmp, p->d_H, p->d_small};
+                    p->d_slot2orig, p->d_bsz, p->d_Dinv, p->d_Gm, p->d_Hm, p->d_Dw, p->d_LU, p->d_lev,
+                    p->d_rscale, p->d_T, p->d_piv, p->d_pidx, p->d_used, p->d_zlo, p->d_xlo, p->d_flo,
+                    p->d_red, p->d_err, p->d_bar, p->d_V, p->d_Vtmp, p->d_small};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     for (auto &v : p->d_v)
@@ -213,16 +213,22 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
     KORE_TRY(upload(p, &p->d_slot2orig, slot2orig));
     KORE_TRY(upload(p, &p->d_bsz, p->bsz));
     KORE_TRY(kore_alloc(p, (void **)&p->d_rscale, p->np * sizeof(double)));
-    KORE_TRY(kore_alloc(p, (void **)&p->d_piv, p->S * sizeof(int)));
-    KORE_TRY(kore_alloc(p, (void **)&p->d_pidx, p->S * sizeof(int)));
-    KORE_TRY(kore_alloc(p, (void **)&p->d_used, p->S * sizeof(int)));
+    kore_build_levels(p);
+    if (!p->lev.empty()) {
+        KORE_TRY(kore_alloc(p, (void **)&p->d_lev, p->lev.size() * sizeof(BcrLevel)));
+        KORE_CUDA_TRY(cudaMemcpy(p->d_lev, p->lev.data(), p->lev.size() * sizeof(BcrLevel), cudaMemcpyHostToDevice));
+    }
+    KORE_TRY(kore_alloc(p, (void **)&p->d_piv, (size_t)p->nodd_max * p->S * sizeof(int)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_pidx, (size_t)p->nodd_max * p->S * sizeof(int)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_used, (size_t)p->nodd_max * p->S * sizeof(int)));
     for (auto &v : p->d_v) KORE_TRY(kore_alloc(p, (void **)&v, p->np * sizeof(double2)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_red, 8192 * sizeof(double)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_err, sizeof(int)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_bar, 64));
     KORE_CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
-    KORE_CUDA_TRY(cudaMemset(p->d_piv, 0, p->S * sizeof(int)));
-    KORE_CUDA_TRY(cudaMemset(p->d_pidx, 0xff, p->S * sizeof(int)));
+    KORE_CUDA_TRY(cudaMemset(p->d_piv, 0, (size_t)p->nodd_max * p->S * sizeof(int)));
+    KORE_CUDA_TRY(cudaMemset(p->d_pidx, 0xff, (size_t)p->nodd_max * p->S * sizeof(int)));
+    KORE_CUDA_TRY(cudaMemset(p->d_used, 0, (size_t)p->nodd_max * p->S * sizeof(int)));
     KORE_CUDA_TRY(cudaMemset(p->d_red, 0, 8192 * sizeof(double)));
     KORE_CUDA_TRY(cudaMallocHost(&p->h_red, 8192 * sizeof(double)));
     KORE_CUDA_TRY(cudaDeviceSynchronize());
@@ -343,12 +349,23 @@ int kore_profile(kore_plan *p, int enable, double *out) {
         out[1] = (double)p->prof_n[0];
         out[2] = p->prof_ms[1];
         out[3] = (double)p->prof_n[1];
-        // one sweep reads Sinv, W, X (K S^2 each), the right-hand side (16 B) and row
-        // scales (8 B), writes/reads z and y in factor precision and writes x (16 B)
-        out[4] = 3.0 * K * S * S * e + np * (16.0 + 8.0 + 16.0) + 4.0 * np * e;
-        // Gauss-Jordan on [S_i | U_i | L_i | I]: sum over panels of the trailing update
-        // 8 * S * nb * (4S - k0 - nb) real flops, i.e. ~8 * S * (4 S^2 - S^2 / 2) per block
-        out[5] = K * 8.0 * S * (4.0 * S * S - 0.5 * S * S);
+        // one sweep reads every D^-1, G, H block once, the dense couplings of the even
+        // blocks of levels >= 1, the level-0 couplings from the CSR (16 B value + 4 B
+        // index per entry), the right-hand side (16 B) and row scales (8 B) and writes x
+        // (16 B); the reduction vectors f, z, x in factor precision are read and written
+        // about twice each
+        double lu = 0.0;
+        for (int l = 1; l < p->nlev; ++l) lu += 2.0 * p->lev[l].neven;
+        out[4] = (3.0 * K + lu) * S * S * e + 20.0 * (double)p->a_nnz + np * (16.0 + 8.0 + 16.0) + 6.0 * np * e;
+        // Gauss-Jordan on [D_j | L_j | U_j | I] for every eliminated block (trailing update
+        // 8 S nb (4S - k0 - nb) real flops per panel, ~28 S^3 per block) and four dense
+        // S^3 complex products (8 S^3 real flops each) per surviving block of levels >= 1
+        double gj = 0.0, gm = 0.0;
+        for (int l = 0; l < p->nlev; ++l) {
+            gj += p->lev[l].nodd;
+            if (l > 0) gm += 4.0 * p->lev[l].neven;
+        }
+        out[5] = (gj + 1.0) * 28.0 * S * S * S + gm * 8.0 * S * S * S;
     }
     if (enable) {
         p->prof_ms[0] = p->prof_ms[1] = 0.0;

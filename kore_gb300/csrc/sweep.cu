@@ -1,15 +1,16 @@
-// Block-tridiagonal sweeps, sparse products and the FP64 refinement loop.
+// Solves with the block-cyclic-reduction factors of factor.cu, sparse products and
+// the FP64 refinement loop.
 //
-// Solve of (A - sigma B) x = b with the factors of factor.cu (R = row scaling):
-//     c   = s^-1 R b                      (s = ||b||_inf keeps complex64 in range)
-//     z_i = S_i^-1 c_i                    all blocks in parallel
-//     y_0 = z_0,      y_i = z_i - W_i y_{i-1}          forward, one block at a time
-//     x_K-1 = y_K-1,  x_i = y_i - X_i x_{i+1}           backward
-//     x  <- s x
-// One cooperative persistent kernel runs the three phases with a bounded grid barrier
-// between dependent blocks.  Each warp owns one row of the current block and
-// prefetches that row of the next block's matrix into registers before it waits at
-// the barrier, so the HBM stream of W_i / X_i overlaps the barrier latency.
+// (A - sigma B) x = b with row scaling R and s = ||b||_inf (keeps complex64 in range):
+// the right-hand side c = s^-1 R b is reduced level by level exactly as the blocks were,
+//     level l, odd blocks j:   z_j = D_j^-1 f_j
+//     level l, even blocks i:  f_i <- f_i - L_i z_jl - U_i z_jr        (CSR couplings at level 0)
+// the last block is solved, x_0 = D_0^-1 f_0, and the levels are unwound in reverse,
+//     level l, odd blocks j:   x_j = z_j - G_j x_jl - H_j x_jr,
+// then x <- s x.  One cooperative persistent kernel runs all phases (about 3 log2 K of
+// them) with a bounded grid barrier between dependent phases; inside a phase every
+// (block, row tile) is independent, so each phase is a batched matrix-vector product
+// streaming the factors from HBM across the whole GPU.
 //
 // In mixed precision the factors are complex64 and the result is refined in FP64:
 //     r = b - (A - sigma B) x,  x += M32^-1 r   until ||r||_inf <= tol (||M||_inf ||x||_inf + ||b||_inf).
@@ -17,103 +18,156 @@
 
 namespace {
 
-constexpr int kSweepThreads = 256;
+constexpr int kSweepThreads = 128;   // one row of a block per thread, 128-row tiles
 
-template <typename C, int MAXT>
-__device__ __forceinline__ void load_row(C (&rv)[MAXT], const C *__restrict__ row, int S, int lane) {
-#pragma unroll
-    for (int t = 0; t < MAXT; ++t) {
-        const int j = lane + 32 * t;
-        rv[t] = (j < S) ? __ldg(row + j) : czero<C>();
-    }
-}
 __device__ __forceinline__ double2 ldcg(const double2 *p) { return __ldcg(p); }
 __device__ __forceinline__ float2 ldcg(const float2 *p) { return __ldcg(p); }
 __device__ __forceinline__ void stcg(double2 *p, double2 v) { __stcg(p, v); }
 __device__ __forceinline__ void stcg(float2 *p, float2 v) { __stcg(p, v); }
 
-template <typename C, int MAXT>
-__global__ void __launch_bounds__(kSweepThreads) k_sweep(
-    int K, int S, const C *__restrict__ Sinv, const C *__restrict__ W, const C *__restrict__ X,
-    const double2 *__restrict__ b, const double *__restrict__ rscale, const double *__restrict__ bnorm,
-    C *__restrict__ z, C *__restrict__ y, double2 *__restrict__ out, int accumulate, unsigned *bar, int *err) {
+// acc += sum_c M[r + c*S] v[c] over c < S (column-major block, vector in shared memory)
+template <typename C>
+__device__ __forceinline__ C colmajor_dot(const C *__restrict__ M, int r, int S, const C *__restrict__ v) {
+    C a0 = czero<C>(), a1 = czero<C>();
+    int c = 0;
+    for (; c + 8 <= S; c += 8) {
+        C m[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) m[t] = __ldg(M + r + (int64_t)(c + t) * S);
+#pragma unroll
+        for (int t = 0; t < 8; t += 2) {
+            a0 = cfma(a0, m[t], v[c + t]);
+            a1 = cfma(a1, m[t + 1], v[c + t + 1]);
+        }
+    }
+    for (; c < S; ++c) a0 = cfma(a0, __ldg(M + r + (int64_t)c * S), v[c]);
+    return a0 + a1;
+}
+
+struct SweepArgs {
+    int K, S, nlev;
+    const BcrLevel *levs;
+    const void *Dinv, *G, *H, *LU;
+    const int *arow, *acol, *asplit;
+    const double2 *aval;
+    const double2 *b;
+    const double *rscale;
+    const double *bnorm;
+    void *f, *z, *x;
+    double2 *out;
+    int accumulate;
+    unsigned *bar;
+    int *err;
+};
+
+template <typename C>
+__global__ void __launch_bounds__(kSweepThreads) k_sweep(SweepArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *vec = reinterpret_cast<C *>(smem_raw);
+    C *v1 = reinterpret_cast<C *>(smem_raw);
+    C *v2 = v1 + a.S;
     GridBarrier gb;
-    gb.init(bar, err);
-    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-    const int gw = blockIdx.x * wpb + (threadIdx.x >> 5), nw = gridDim.x * wpb;
+    gb.init(a.bar, a.err);
+    const int S = a.S;
     const int64_t SS = (int64_t)S * S;
-    const double bn = *bnorm;
+    const int ntile = (S + kSweepThreads - 1) / kSweepThreads;
+    const C *Dinv = static_cast<const C *>(a.Dinv), *G = static_cast<const C *>(a.G);
+    const C *H = static_cast<const C *>(a.H), *LU = static_cast<const C *>(a.LU);
+    C *f = static_cast<C *>(a.f), *z = static_cast<C *>(a.z), *x = static_cast<C *>(a.x);
+    const double bn = *a.bnorm;
     const double bscale = (bn > 0.0) ? 1.0 / bn : 1.0;
     const double oscale = (bn > 0.0) ? bn : 1.0;
+    const int tid = threadIdx.x;
+    auto rhs0 = [&](int64_t p) -> C { return from_c128<C>((a.rscale[p] * bscale) * a.b[p]); };
+    auto emit = [&](int64_t p, C v) {
+        stcg(x + p, v);
+        const double2 d = oscale * to_c128(v);
+        a.out[p] = a.accumulate ? a.out[p] + d : d;
+    };
 
-    // phase 1: z = Sinv c, every row of every block
-    for (int64_t row = gw; row < (int64_t)K * S; row += nw) {
-        const int64_t i = row / S;
-        const int k = (int)(row - i * S);
-        const C *a = Sinv + i * SS + (int64_t)k * S;
-        const double2 *bb = b + i * S;
-        const double *rs = rscale + i * S;
-        C acc = czero<C>();
-        for (int j = lane; j < S; j += 32) acc = cfma(acc, __ldg(a + j), from_c128<C>((rs[j] * bscale) * bb[j]));
-        acc = warp_sum(acc);
-        if (lane == 0) stcg(z + row, acc);
-    }
-    const bool own = gw < S;
-    C rv[MAXT];
-    if (own) {
-        stcg(y + gw, ldcg(z + gw));  // y_0 = z_0 (after the barrier everybody reads it)
-        if (K > 1) load_row<C, MAXT>(rv, W + SS + (int64_t)gw * S, S, lane);
-    }
-    gb.sync();  // z complete, y_0 complete
-    // phase 2: forward
-    for (int i = 1; i < K; ++i) {
-        for (int j = threadIdx.x; j < S; j += blockDim.x) vec[j] = ldcg(y + (int64_t)(i - 1) * S + j);
-        __syncthreads();
-        if (own) {
-            C acc = czero<C>();
-#pragma unroll
-            for (int t = 0; t < MAXT; ++t) {
-                const int j = lane + 32 * t;
-                if (j < S) acc = cfma(acc, rv[t], vec[j]);
+    // ---------------------------------------------------------------- reduction
+    for (int l = 0; l < a.nlev; ++l) {
+        const BcrLevel lv = a.levs[l];
+        // phase A: z_j = Dinv_j f_j for the odd blocks
+        for (int64_t it = blockIdx.x; it < (int64_t)lv.nodd * ntile; it += gridDim.x) {
+            const int64_t o = it / ntile;
+            const int tile = (int)(it - o * ntile);
+            const int64_t j = (2 * o + 1) * lv.stride;
+            __syncthreads();
+            for (int c = tid; c < S; c += blockDim.x) v1[c] = (l == 0) ? rhs0(j * S + c) : ldcg(f + j * S + c);
+            __syncthreads();
+            const int r = tile * kSweepThreads + tid;
+            if (r < S) stcg(z + j * S + r, colmajor_dot(Dinv + j * SS, r, S, v1));
+        }
+        gb.sync();
+        // phase B: f_i -= L_i z_jl + U_i z_jr for the even blocks
+        for (int64_t it = blockIdx.x; it < (int64_t)lv.neven * ntile; it += gridDim.x) {
+            const int64_t e = it / ntile;
+            const int tile = (int)(it - e * ntile);
+            const int64_t q = 2 * e, i = q * lv.stride;
+            const bool hasl = q >= 1, hasr = q + 1 < lv.Kl;
+            const int64_t jl = (q - 1) * lv.stride, jr = (q + 1) * lv.stride;
+            const int r = tile * kSweepThreads + tid;
+            if (l == 0) {
+                if (r < S) {
+                    const int64_t p = i * S + r;
+                    C acc = czero<C>();
+                    const double rs = a.rscale[p];
+                    if (hasl)
+                        for (int k = a.arow[p]; k < a.asplit[2 * p]; ++k)
+                            acc = cfma(acc, from_c128<C>(rs * a.aval[k]), ldcg(z + a.acol[k]));
+                    if (hasr)
+                        for (int k = a.asplit[2 * p + 1]; k < a.arow[p + 1]; ++k)
+                            acc = cfma(acc, from_c128<C>(rs * a.aval[k]), ldcg(z + a.acol[k]));
+                    stcg(f + p, rhs0(p) - acc);
+                }
+            } else {
+                __syncthreads();
+                for (int c = tid; c < S; c += blockDim.x) {
+                    v1[c] = hasl ? ldcg(z + jl * S + c) : czero<C>();
+                    v2[c] = hasr ? ldcg(z + jr * S + c) : czero<C>();
+                }
+                __syncthreads();
+                if (r < S) {
+                    C acc = czero<C>();
+                    if (hasl) acc = colmajor_dot(LU + (lv.lu_L + q) * SS, r, S, v1);
+                    if (hasr) acc = acc + colmajor_dot(LU + (lv.lu_U + q) * SS, r, S, v2);
+                    stcg(f + i * S + r, ldcg(f + i * S + r) - acc);
+                }
             }
-            acc = warp_sum(acc);
-            if (lane == 0) stcg(y + (int64_t)i * S + gw, ldcg(z + (int64_t)i * S + gw) - acc);
-            if (i + 1 < K) load_row<C, MAXT>(rv, W + (int64_t)(i + 1) * SS + (int64_t)gw * S, S, lane);
         }
         gb.sync();
     }
-    // phase 3: backward (x overwrites y)
-    if (own) {
-        const int64_t idx = (int64_t)(K - 1) * S + gw;
-        if (lane == 0) {
-            const double2 v = oscale * to_c128(ldcg(y + idx));
-            out[idx] = accumulate ? out[idx] + v : v;
-        }
-        if (K > 1) load_row<C, MAXT>(rv, X + (int64_t)(K - 2) * SS + (int64_t)gw * S, S, lane);
-    }
-    for (int i = K - 2; i >= 0; --i) {
-        for (int j = threadIdx.x; j < S; j += blockDim.x) vec[j] = ldcg(y + (int64_t)(i + 1) * S + j);
+    // ---------------------------------------------------------------- top block
+    for (int64_t it = blockIdx.x; it < ntile; it += gridDim.x) {
         __syncthreads();
-        if (own) {
-            C acc = czero<C>();
-#pragma unroll
-            for (int t = 0; t < MAXT; ++t) {
-                const int j = lane + 32 * t;
-                if (j < S) acc = cfma(acc, rv[t], vec[j]);
-            }
-            acc = warp_sum(acc);
-            if (lane == 0) {
-                const int64_t idx = (int64_t)i * S + gw;
-                const C xv = ldcg(y + idx) - acc;
-                stcg(y + idx, xv);
-                const double2 v = oscale * to_c128(xv);
-                out[idx] = accumulate ? out[idx] + v : v;
-            }
-            if (i > 0) load_row<C, MAXT>(rv, X + (int64_t)(i - 1) * SS + (int64_t)gw * S, S, lane);
-        }
+        for (int c = tid; c < S; c += blockDim.x) v1[c] = (a.nlev == 0) ? rhs0(c) : ldcg(f + c);
+        __syncthreads();
+        const int r = (int)it * kSweepThreads + tid;
+        if (r < S) emit(r, colmajor_dot(Dinv, r, S, v1));
+    }
+    // ---------------------------------------------------------------- back substitution
+    for (int l = a.nlev - 1; l >= 0; --l) {
         gb.sync();
+        const BcrLevel lv = a.levs[l];
+        for (int64_t it = blockIdx.x; it < (int64_t)lv.nodd * ntile; it += gridDim.x) {
+            const int64_t o = it / ntile;
+            const int tile = (int)(it - o * ntile);
+            const int64_t q = 2 * o + 1, j = q * lv.stride;
+            const bool hasr = q + 1 < lv.Kl;
+            const int64_t jl = j - lv.stride, jr = j + lv.stride;
+            __syncthreads();
+            for (int c = tid; c < S; c += blockDim.x) {
+                v1[c] = ldcg(x + jl * S + c);
+                v2[c] = hasr ? ldcg(x + jr * S + c) : czero<C>();
+            }
+            __syncthreads();
+            const int r = tile * kSweepThreads + tid;
+            if (r < S) {
+                C acc = colmajor_dot(G + j * SS, r, S, v1);
+                if (hasr) acc = acc + colmajor_dot(H + j * SS, r, S, v2);
+                emit(j * S + r, ldcg(z + j * S + r) - acc);
+            }
+        }
     }
 }
 
@@ -220,35 +274,32 @@ __global__ void k_scatter(int64_t np, const int64_t *__restrict__ s2o, const dou
     }
 }
 
-template <typename C, int MAXT>
-int launch_sweep_t(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int accumulate) {
-    auto kern = k_sweep<C, MAXT>;
-    const size_t smem = (size_t)p->S * sizeof(C);
-    const C *Sinv = static_cast<const C *>(p->d_sinv);
-    const C *W = static_cast<const C *>(p->d_W);
-    const C *X = static_cast<const C *>(p->d_X);
-    C *z = static_cast<C *>(p->d_zlo);
-    C *y = static_cast<C *>(p->d_ylo);
-    int K = p->K, S = p->S;
+template <typename C>
+int launch_sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int accumulate) {
+    SweepArgs a;
+    a.K = p->K; a.S = p->S; a.nlev = p->nlev; a.levs = p->d_lev;
+    a.Dinv = p->d_Dinv; a.G = p->d_Gm; a.H = p->d_Hm; a.LU = p->d_LU;
+    a.arow = p->d_arow; a.acol = p->d_acol; a.asplit = p->d_asplit; a.aval = p->d_aval;
+    a.b = b; a.rscale = p->d_rscale; a.bnorm = bnorm;
+    a.f = p->d_flo; a.z = p->d_zlo; a.x = p->d_xlo;
+    a.out = x; a.accumulate = accumulate; a.bar = p->d_bar; a.err = p->d_err;
+    const size_t smem = 2 * (size_t)p->S * sizeof(C);
+    auto kern = k_sweep<C>;
+    const int ti = (sizeof(C) == 16) ? 1 : 0;
+    if (p->sweep_occ[ti] == 0) {
+        if (smem > 48 * 1024)
+            KORE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int occ = 0;
+        KORE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kSweepThreads, smem));
+        p->sweep_occ[ti] = std::max(1, std::min(occ, 8));
+    }
+    const int occ = p->sweep_occ[ti];
     KORE_CUDA_TRY(cudaMemsetAsync(p->d_bar, 0, sizeof(unsigned), p->stream));
-    void *args[] = {&K, &S, (void *)&Sinv, (void *)&W, (void *)&X, (void *)&b, (void *)&p->d_rscale,
-                    (void *)&bnorm, (void *)&z, (void *)&y, (void *)&x, &accumulate, (void *)&p->d_bar,
-                    (void *)&p->d_err};
-    dim3 grid(p->num_sms), block(kSweepThreads);
+    void *args[] = {&a};
+    dim3 grid(p->num_sms * occ), block(kSweepThreads);
     KORE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)kern, grid, block, args, smem, p->stream));
     KORE_LAUNCHED(1);
     return KORE_OK;
-}
-
-template <typename C>
-int launch_sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int accumulate) {
-    const int S = p->S;
-    if (S <= 64) return launch_sweep_t<C, 2>(p, b, bnorm, x, accumulate);
-    if (S <= 128) return launch_sweep_t<C, 4>(p, b, bnorm, x, accumulate);
-    if (S <= 256) return launch_sweep_t<C, 8>(p, b, bnorm, x, accumulate);
-    if (S <= 512) return launch_sweep_t<C, 16>(p, b, bnorm, x, accumulate);
-    if (S <= 1024) return launch_sweep_t<C, 32>(p, b, bnorm, x, accumulate);
-    return KORE_EINVAL;
 }
 
 int sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int accumulate) {
