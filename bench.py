@@ -347,7 +347,9 @@ def main():
                      "peak_source": src, "traffic": None, "bytes_per_launch": prof["sweep_bytes"],
                      "avg_launch_ms": sweep_ms, "launches": prof["sweeps"],
                      "sweep_share_of_step": prof["sweep_ms"] / total_ms,
-                     "factor_ms_avg": prof["factor_ms"] / max(prof["factors"], 1)},
+                     "factor_ms_avg": prof["factor_ms"] / max(prof["factors"], 1),
+                     "step_breakdown_ms": {k: prof[k] / args.steps for k in ("sweep_ms", "factor_ms", "spmv_ms",
+                                                                            "ortho_ms", "schur_ms")}},
         "clocks": clocks.summary(),
         "e2e": e2e,
     }

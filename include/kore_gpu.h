@@ -148,9 +148,10 @@ int kore_plan_stream(const kore_plan *plan, void **stream);
 
 /*
  * Kernel timing with CUDA events on the plan's stream.  enable = 1 starts recording
- * (and clears the totals), 0 stops.  out (may be NULL) receives 6 doubles:
- * [sweep kernel ms total, sweep launches, factorisation ms total, factorisations,
- *  algorithmic bytes of one sweep launch, algorithmic flops of one factorisation].
+ * (and clears the totals), 0 stops.  out (may be NULL) receives 12 doubles:
+ * [sweep kernel ms total, sweeps that ran, factorisation ms total, factorisations,
+ *  algorithmic bytes of one sweep launch, algorithmic flops of one factorisation,
+ *  sparse-product ms, count, orthogonalisation ms, count, projected-problem ms, count].
  */
 int kore_profile(kore_plan *plan, int enable, double *out);
 

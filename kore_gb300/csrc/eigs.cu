@@ -25,7 +25,6 @@
 namespace {
 
 constexpr int kMaxNcv = 64;
-constexpr int kSchurThreads = 128;
 
 // ----------------------------------------------------------------------------- sort keys
 // Ascending key = wanted first (the comparison functions of SLEPc's `which`).
@@ -98,22 +97,88 @@ __device__ inline double2 csqrt_(double2 z) {
     return mk(fabs(z.y) / (2.0 * t), copysign(t, z.y));
 }
 
-// One CTA.  Hbar: (m+1) x m column-major (ld m+1); row m holds the residual row.
-__global__ void __launch_bounds__(kSchurThreads) k_schur(const double2 *__restrict__ Hbar, int m, int which,
-                                                         double tre, double tim, SchurOut out) {
+__device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
+
+// G = [c s; -conj(s) c] with G [x; y] = [r; 0]; c = |x| / n, s = (x / |x|) conj(y) / n,
+// n = sqrt(|x|^2 + |y|^2), evaluated with two reciprocal square roots.
+__device__ __forceinline__ void givens_r(double2 x, double2 y, double &c, double2 &s) {
+    const double a2 = abs2(x), b2 = abs2(y);
+    if (b2 == 0.0) { c = 1.0; s = mk(0.0, 0.0); return; }
+    if (a2 == 0.0) { c = 0.0; s = mk(1.0, 0.0); return; }
+    const double rn = rsqrt(a2 + b2), ra = rsqrt(a2);
+    c = a2 * ra * rn;
+    s = (ra * rn) * (x * conjg(y));
+}
+
+// Apply G from the left to rows k, k+1 and G^H from the right to columns k, k+1 of H
+// (rows [0, r1), columns [c0, m)), and G^H to columns k, k+1 of Q, in one parallel step.
+// The 2 x 2 block where the row and column updates meet is done by one thread.
+__device__ __forceinline__ void apply_rot(double2 *H, double2 *Q, int m, int k, int c0, int r1, double c, double2 s) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int nrow = m - (k + 2);                     // columns k+2.. of rows k, k+1
+    const int ncol = (r1 > k) ? k : r1;                // rows 0..k-1 of columns k, k+1
+    const int nlow = (r1 > k + 2) ? 1 : 0;             // row k+2 of columns k, k+1
+    const int nleft = (c0 < k) ? 1 : 0;                // column k-1 of rows k, k+1
+    const int total = nrow + ncol + nlow + nleft + m + 1;
+    for (int t = tid; t < total; t += nt) {
+        int u = t;
+        if (u < nrow) {
+            const int j = k + 2 + u;
+            const double2 a = H[k + j * m], b = H[k + 1 + j * m];
+            H[k + j * m] = c * a + s * b;
+            H[k + 1 + j * m] = c * b - conjg(s) * a;
+            continue;
+        }
+        u -= nrow;
+        if (u < ncol + nlow) {
+            const int i = (u < ncol) ? u : k + 2;
+            const double2 a = H[i + k * m], b = H[i + (k + 1) * m];
+            H[i + k * m] = c * a + b * conjg(s);
+            H[i + (k + 1) * m] = c * b - a * s;
+            continue;
+        }
+        u -= ncol + nlow;
+        if (u < nleft) {
+            const int j = k - 1;
+            const double2 a = H[k + j * m], b = H[k + 1 + j * m];
+            H[k + j * m] = c * a + s * b;
+            H[k + 1 + j * m] = c * b - conjg(s) * a;
+            continue;
+        }
+        u -= nleft;
+        if (u < m) {
+            const double2 a = Q[u + k * m], b = Q[u + (k + 1) * m];
+            Q[u + k * m] = c * a + b * conjg(s);
+            Q[u + (k + 1) * m] = c * b - a * s;
+            continue;
+        }
+        // the 2 x 2 block: rows then columns
+        double2 h00 = H[k + k * m], h01 = H[k + (k + 1) * m], h10 = H[k + 1 + k * m], h11 = H[k + 1 + (k + 1) * m];
+        double2 t00 = c * h00 + s * h10, t01 = c * h01 + s * h11;
+        double2 t10 = c * h10 - conjg(s) * h00, t11 = c * h11 - conjg(s) * h01;
+        H[k + k * m] = c * t00 + t01 * conjg(s);
+        H[k + (k + 1) * m] = c * t01 - t00 * s;
+        H[k + 1 + k * m] = c * t10 + t11 * conjg(s);
+        H[k + 1 + (k + 1) * m] = c * t11 - t10 * s;
+    }
+}
+
+// One CTA of 128 threads (four warps, one per SM sub-partition, so the FP64 updates
+// of a rotation run on all four FP64 pipes).  Hbar: (m+1) x m column-major (ld m+1);
+// row m is the residual row.
+constexpr int kSchurT = 128;
+__global__ void __launch_bounds__(kSchurT) k_schur(const double2 *__restrict__ Hbar, int m, int which, double tre,
+                                                   double tim, SchurOut out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2 *H = reinterpret_cast<double2 *>(smem_raw);  // m x m
     double2 *Q = H + m * m;                               // m x m
     double2 *Y = Q + m * m;                               // m x m
     __shared__ double2 vsh[kMaxNcv];
-    __shared__ double2 red[kMaxNcv];
-    __shared__ double s_c;
-    __shared__ double2 s_s;
-    __shared__ int s_flag, s_l, s_j;
-    __shared__ double2 s_mu;
-    const int tid = threadIdx.x;
+    __shared__ double key[kMaxNcv];
+    __shared__ double red[4];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int ldh = m + 1;
-    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+    for (int idx = tid; idx < m * m; idx += kSchurT) {
         const int r = idx % m, c = idx / m;
         H[idx] = Hbar[r + c * ldh];
         Q[idx] = (r == c) ? mk(1.0, 0.0) : mk(0.0, 0.0);
@@ -123,48 +188,45 @@ __global__ void __launch_bounds__(kSchurThreads) k_schur(const double2 *__restri
     // --- Householder reduction to upper Hessenberg form
     for (int k = 0; k + 2 < m; ++k) {
         const int len = m - k - 1;
-        if (tid == 0) {
-            double xn = 0.0;
-            for (int i = 0; i < len; ++i) xn += abs2(H[k + 1 + i + k * m]);
-            double tail = xn - abs2(H[k + 1 + k * m]);
-            s_flag = (tail > 0.0) ? 1 : 0;
-            if (s_flag) {
-                xn = sqrt(xn);
-                const double2 x0 = H[k + 1 + k * m];
-                const double a0 = cabs_(x0);
-                const double2 ph = (a0 > 0.0) ? mk(x0.x / a0, x0.y / a0) : mk(1.0, 0.0);
-                // v = x + ph*||x|| e1 ; H x -> -ph ||x|| e1
-                double vn = 0.0;
-                for (int i = 0; i < len; ++i) {
-                    double2 v = H[k + 1 + i + k * m];
-                    if (i == 0) v = v + xn * ph;
-                    vsh[i] = v;
-                    vn += abs2(v);
-                }
-                vn = sqrt(vn);
-                for (int i = 0; i < len; ++i) vsh[i] = (1.0 / vn) * vsh[i];
-            }
+        double sq = 0.0;
+        for (int i = tid; i < len; i += kSchurT) sq += abs2(H[k + 1 + i + k * m]);
+        sq = warp_sum_d(sq);
+        if (lane == 0) red[wid] = sq;
+        __syncthreads();
+        sq = red[0] + red[1] + red[2] + red[3];
+        const double2 x0 = H[k + 1 + k * m];
+        __syncthreads();
+        if (!(sq - abs2(x0) > 0.0)) continue;
+        const double xn = sqrt(sq);
+        const double a0 = cabs_(x0);
+        const double2 ph = (a0 > 0.0) ? mk(x0.x / a0, x0.y / a0) : mk(1.0, 0.0);
+        // v = x + ph ||x|| e1, ||v||^2 = 2 ||x|| (||x|| + |x0|)
+        const double vinv = rsqrt(2.0 * xn * (xn + a0));
+        for (int i = tid; i < len; i += kSchurT) {
+            double2 v = H[k + 1 + i + k * m];
+            if (i == 0) v = v + xn * ph;
+            vsh[i] = vinv * v;
         }
         __syncthreads();
-        if (!s_flag) continue;
-        // H <- (I - 2 v v^H) H   (rows k+1.., columns k..)
-        for (int c = k + tid; c < m; c += blockDim.x) {
-            double2 s = mk(0.0, 0.0);
-            for (int i = 0; i < len; ++i) s = cfmaconj(s, vsh[i], H[k + 1 + i + c * m]);
-            for (int i = 0; i < len; ++i) H[k + 1 + i + c * m] = H[k + 1 + i + c * m] - 2.0 * (vsh[i] * s);
+        // H <- (I - 2 v v^H) H (rows k+1.., columns k..), one column per thread
+        for (int c = k + tid; c < m; c += kSchurT) {
+            double2 t = mk(0.0, 0.0);
+            for (int i = 0; i < len; ++i) t = cfmaconj(t, vsh[i], H[k + 1 + i + c * m]);
+            t = 2.0 * t;
+            for (int i = 0; i < len; ++i) H[k + 1 + i + c * m] = cfms(H[k + 1 + i + c * m], vsh[i], t);
         }
         __syncthreads();
-        // H <- H (I - 2 v v^H),  Q <- Q (I - 2 v v^H)   (all rows, columns k+1..)
-        for (int r = tid; r < 2 * m; r += blockDim.x) {
+        // H <- H (I - 2 v v^H), Q <- Q (I - 2 v v^H): one row per thread
+        for (int r = tid; r < 2 * m; r += kSchurT) {
             double2 *M = (r < m) ? H : Q;
             const int rr = (r < m) ? r : r - m;
-            double2 s = mk(0.0, 0.0);
-            for (int i = 0; i < len; ++i) s = cfma(s, M[rr + (k + 1 + i) * m], vsh[i]);
-            for (int i = 0; i < len; ++i)
-                M[rr + (k + 1 + i) * m] = M[rr + (k + 1 + i) * m] - 2.0 * (s * conjg(vsh[i]));
+            double2 t = mk(0.0, 0.0);
+            for (int i = 0; i < len; ++i) t = cfma(t, M[rr + (k + 1 + i) * m], vsh[i]);
+            t = 2.0 * t;
+            for (int i = 0; i < len; ++i) M[rr + (k + 1 + i) * m] = cfms(M[rr + (k + 1 + i) * m], t, conjg(vsh[i]));
         }
         __syncthreads();
-        if (tid == 0) for (int i = 2; i < len + 1; ++i) H[k + i + k * m] = mk(0.0, 0.0);
+        for (int i = 2 + tid; i < len + 1; i += kSchurT) H[k + i + k * m] = mk(0.0, 0.0);
         __syncthreads();
     }
 
@@ -172,117 +234,98 @@ __global__ void __launch_bounds__(kSchurThreads) k_schur(const double2 *__restri
     const double eps = 2.220446049250313e-16;
     int hi = m - 1, iter = 0, total = 0, fail = 0;
     while (hi > 0) {
-        if (tid == 0) {
-            int l = hi;
-            while (l > 0) {
-                const double hs = cabs_(H[l + (l - 1) * m]);
-                double ref = cabs_(H[l - 1 + (l - 1) * m]) + cabs_(H[l + l * m]);
-                if (ref == 0.0) ref = 1.0;
-                if (hs <= eps * ref) { H[l + (l - 1) * m] = mk(0.0, 0.0); break; }
-                --l;
-            }
-            s_l = l;
-            if (l < hi) {
-                const double2 a = H[hi - 1 + (hi - 1) * m], b = H[hi - 1 + hi * m];
-                const double2 c = H[hi + (hi - 1) * m], d = H[hi + hi * m];
-                double2 mu;
-                if (iter > 0 && iter % 10 == 0) {
-                    // exceptional shift
-                    mu = d + mk(1.5 * fabs(c.x), 0.0);
-                } else {
-                    const double2 half = 0.5 * (a - d);
-                    const double2 disc = csqrt_(half * half + b * c);
-                    const double2 m1 = 0.5 * (a + d) + disc, m2 = 0.5 * (a + d) - disc;
-                    mu = (abs2(m1 - d) < abs2(m2 - d)) ? m1 : m2;
-                }
-                s_mu = mu;
-            }
+        int l = hi;
+        while (l > 0) {
+            double ref = cabs1(H[l - 1 + (l - 1) * m]) + cabs1(H[l + l * m]);
+            if (ref == 0.0) ref = 1.0;
+            if (cabs1(H[l + (l - 1) * m]) <= eps * ref) break;
+            --l;
         }
         __syncthreads();
-        const int l = s_l;
+        if (l > 0 && tid == 0) H[l + (l - 1) * m] = mk(0.0, 0.0);
+        __syncthreads();
         if (l == hi) { --hi; iter = 0; continue; }
         if (++total > 60 * m) { fail = 1; break; }
         ++iter;
-        const double2 mu = s_mu;
-        for (int k = l; k < hi; ++k) {
-            if (tid == 0) {
-                double2 x, y;
-                if (k == l) { x = H[l + l * m] - mu; y = H[l + 1 + l * m]; }
-                else { x = H[k + (k - 1) * m]; y = H[k + 1 + (k - 1) * m]; }
-                double c; double2 s;
-                givens(x, y, c, s);
-                s_c = c; s_s = s;
+        double2 mu;
+        {
+            const double2 a = H[hi - 1 + (hi - 1) * m], b = H[hi - 1 + hi * m];
+            const double2 c = H[hi + (hi - 1) * m], d = H[hi + hi * m];
+            if (iter % 10 == 0) {
+                mu = d + mk(1.5 * fabs(c.x), 0.0);   // exceptional shift
+            } else {
+                const double2 half = 0.5 * (a - d);
+                const double2 disc = csqrt_(half * half + b * c);
+                const double2 m1 = 0.5 * (a + d) + disc, m2 = 0.5 * (a + d) - disc;
+                mu = (abs2(m1 - d) < abs2(m2 - d)) ? m1 : m2;
             }
-            __syncthreads();
-            const double c = s_c; const double2 s = s_s;
-            rot_rows(H, m, k, (k > l) ? k - 1 : l, m, c, s);
-            __syncthreads();
-            rot_cols(H, m, k, 0, min(k + 3, hi + 1), c, s);
-            rot_cols(Q, m, k, 0, m, c, s);
-            __syncthreads();
-            if (tid == 0 && k > l) H[k + 1 + (k - 1) * m] = mk(0.0, 0.0);
-            __syncthreads();
         }
+        for (int k = l; k < hi; ++k) {
+            double2 x, y;
+            if (k == l) { x = H[l + l * m] - mu; y = H[l + 1 + l * m]; }
+            else { x = H[k + (k - 1) * m]; y = H[k + 1 + (k - 1) * m]; }
+            double c; double2 sn;
+            givens_r(x, y, c, sn);
+            __syncthreads();
+            apply_rot(H, Q, m, k, (k > l) ? k - 1 : l, min(k + 3, hi + 1), c, sn);
+            __syncthreads();
+            if (k > l && tid == 0) H[k + 1 + (k - 1) * m] = mk(0.0, 0.0);
+        }
+        __syncthreads();
     }
-    // clean the strictly lower part
-    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+    for (int idx = tid; idx < m * m; idx += kSchurT) {
         const int r = idx % m, c = idx / m;
         if (r > c) H[idx] = mk(0.0, 0.0);
     }
     __syncthreads();
 
-    // --- order the diagonal by the `which` key (selection by adjacent swaps)
+    // --- order the diagonal by the `which` key: selection by adjacent swaps (Givens)
+    for (int j = tid; j < m; j += kSchurT) key[j] = which_key(H[j + j * m], which, tre, tim);
+    __syncthreads();
     for (int pos = 0; pos < m; ++pos) {
-        if (tid == 0) {
-            int best = pos;
-            double bk = which_key(H[pos + pos * m], which, tre, tim);
-            for (int j = pos + 1; j < m; ++j) {
-                const double kj = which_key(H[j + j * m], which, tre, tim);
-                if (kj < bk) { bk = kj; best = j; }
-            }
-            s_j = best;
-        }
-        __syncthreads();
-        for (int k = s_j - 1; k >= pos; --k) {
+        int best = pos;
+        double bk = key[pos];
+        for (int j = pos + 1; j < m; ++j)
+            if (key[j] < bk) { bk = key[j]; best = j; }
+        for (int k = best - 1; k >= pos; --k) {
+            const double2 t11 = H[k + k * m], t22 = H[k + 1 + (k + 1) * m], t12 = H[k + (k + 1) * m];
+            double c; double2 sn;
+            givens_r(t12, t22 - t11, c, sn);
+            __syncthreads();
+            apply_rot(H, Q, m, k, k, k + 2, c, sn);
+            __syncthreads();
             if (tid == 0) {
-                const double2 t11 = H[k + k * m], t22 = H[k + 1 + (k + 1) * m], t12 = H[k + (k + 1) * m];
-                double c; double2 s;
-                givens(t12, t22 - t11, c, s);
-                s_c = c; s_s = s;
+                H[k + 1 + k * m] = mk(0.0, 0.0);
+                const double t = key[k];
+                key[k] = key[k + 1];
+                key[k + 1] = t;
             }
-            __syncthreads();
-            const double c = s_c; const double2 s = s_s;
-            rot_rows(H, m, k, k, m, c, s);
-            __syncthreads();
-            rot_cols(H, m, k, 0, k + 2, c, s);
-            rot_cols(Q, m, k, 0, m, c, s);
-            __syncthreads();
-            if (tid == 0) H[k + 1 + k * m] = mk(0.0, 0.0);
             __syncthreads();
         }
     }
 
     // --- eigenvectors of T (one thread per eigenvalue), Ritz estimates
-    const double beta = Hbar[m + (m - 1) * ldh].x;   // real, >= 0, and only entry of the residual row
-    for (int j = tid; j < m; j += blockDim.x) {
+    const double beta = Hbar[m + (m - 1) * ldh].x;   // the only entry of the residual row
+    for (int j = tid; j < m; j += kSchurT) {
         const double2 lam = H[j + j * m];
-        double smin = eps * cabs_(lam);
+        double smin = eps * cabs1(lam);
         if (smin == 0.0) smin = 1e-300;
-        for (int i = 0; i < m; ++i) Y[i + j * m] = mk(0.0, 0.0);
+        for (int i = j + 1; i < m; ++i) Y[i + j * m] = mk(0.0, 0.0);
         Y[j + j * m] = mk(1.0, 0.0);
         for (int i = j - 1; i >= 0; --i) {
             double2 s = mk(0.0, 0.0);
             for (int l2 = i + 1; l2 <= j; ++l2) s = cfma(s, H[i + l2 * m], Y[l2 + j * m]);
             double2 den = H[i + i * m] - lam;
-            if (cabs_(den) < smin) den = mk(smin, 0.0);
-            Y[i + j * m] = -cdiv(s, den);
+            if (cabs1(den) < smin) den = mk(smin, 0.0);
+            const double dinv = 1.0 / abs2(den);
+            Y[i + j * m] = -(dinv * (s * conjg(den)));
         }
         double yn = 0.0;
         for (int i = 0; i <= j; ++i) yn += abs2(Y[i + j * m]);
-        yn = sqrt(yn);
+        const double yinv = rsqrt(yn);
         double2 bt = mk(0.0, 0.0);
         for (int i = 0; i <= j; ++i) {
-            Y[i + j * m] = (1.0 / yn) * Y[i + j * m];
+            Y[i + j * m] = yinv * Y[i + j * m];
             bt = cfma(bt, Q[(m - 1) + i * m], Y[i + j * m]);
         }
         const double th = cabs_(lam);
@@ -291,7 +334,7 @@ __global__ void __launch_bounds__(kSchurThreads) k_schur(const double2 *__restri
         out.bnew[j] = beta * Q[(m - 1) + j * m];
     }
     __syncthreads();
-    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+    for (int idx = tid; idx < m * m; idx += kSchurT) {
         out.T[idx] = H[idx];
         out.Q[idx] = Q[idx];
         out.Y[idx] = Y[idx];
@@ -477,21 +520,16 @@ static void start_vector(int64_t n, uint64_t seed, std::vector<double2> &v) {
     }
 }
 
-int apply_op(Ctx &c, const double2 *v, double2 *out, kore_stats *st, int *iters_max, double *res_max) {
+int apply_op(Ctx &c, const double2 *v, double2 *out) {
     KORE_TRY(kore_spmv_b(c.p, v, c.t1));
-    int it = 0;
-    double res = 0.0;
-    KORE_TRY(kore_apply_inverse(c.p, c.t1, out, c.refine_tol, &it, &res));
-    if (st) { st->op_applies++; st->sweeps += (it > 0 ? it : 1); }
-    *iters_max = std::max(*iters_max, it);
-    *res_max = std::max(*res_max, res);
-    return KORE_OK;
+    return kore_apply_inverse(c.p, c.t1, out, c.refine_tol);
 }
 
 // orthogonalise w against V[:, 0:ncol] twice, write h and beta into Hbar column j,
 // v_{j+1} = w / beta
 int orthonormalise(Ctx &c, int ncol, int j, int ldh) {
     kore_plan *p = c.p;
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 3, true));
     for (int pass = 0; pass < 2; ++pass) {
         k_mdot<<<c.grid, kDotThreads, 0, p->stream>>>(c.np, ncol, c.V, c.w, c.partial);
         k_mdot_reduce<<<ncol, 256, 0, p->stream>>>((int)c.grid, ncol, c.partial, c.h + (pass ? kMaxNcv + 1 : 0), 0);
@@ -504,6 +542,7 @@ int orthonormalise(Ctx &c, int ncol, int j, int ldh) {
     k_finish_col<<<1, 256, 0, p->stream>>>((int)c.grid, c.dpart, c.h, ncol, c.Hbar, ldh, j, c.beta);
     k_scale_copy<<<c.grid, 256, 0, p->stream>>>(c.np, c.w, c.beta, c.V + (int64_t)(j + 1) * c.np);
     KORE_LAUNCHED(4);
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 3, false));
     KORE_CUDA_TRY(cudaGetLastError());
     return KORE_OK;
 }
@@ -572,19 +611,20 @@ int kore_eigs_impl(kore_plan *p, const kore_eps_opts *o, double *evals, double *
     std::vector<double2> h_theta(m);
     int h_info = 0;
     int kkeep = 0, nconv = 0, restarts = 0;
-    int iters_max = 0;
-    double res_max = 0.0;
     c.refine_tol = o->refine_tol;
+    KORE_TRY(kore_ir_reset(p));
     for (restarts = 0;; ++restarts) {
         // Arnoldi expansion kkeep .. m-1
         for (int j = kkeep; j < m; ++j) {
-            KORE_TRY(apply_op(c, c.V + (int64_t)j * np, c.w, st, &iters_max, &res_max));
+            KORE_TRY(apply_op(c, c.V + (int64_t)j * np, c.w));
             KORE_TRY(orthonormalise(c, j + 1, j, ldh));
         }
+        if (p->prof) KORE_TRY(kore_prof_mark(p, 4, true));
         SchurOut so{dT, dQ, dY, dtheta, dest, dbnew, dinfo};
-        k_schur<<<1, kSchurThreads, schur_smem, p->stream>>>(c.Hbar, m, o->which, o->target_re, o->target_im, so);
+        k_schur<<<1, kSchurT, schur_smem, p->stream>>>(c.Hbar, m, o->which, o->target_re, o->target_im, so);
         KORE_LAUNCHED(1);
         KORE_CUDA_TRY(cudaGetLastError());
+        if (p->prof) KORE_TRY(kore_prof_mark(p, 4, false));
         KORE_CUDA_TRY(cudaMemcpyAsync(h_est.data(), dest, m * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
         KORE_CUDA_TRY(cudaMemcpyAsync(h_theta.data(), dtheta, m * sizeof(double2), cudaMemcpyDeviceToHost, p->stream));
         KORE_CUDA_TRY(cudaMemcpyAsync(&h_info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
@@ -597,11 +637,13 @@ int kore_eigs_impl(kore_plan *p, const kore_eps_opts *o, double *evals, double *
         // thick restart
         const int l = std::max(1, (m - nconv) / 2);
         const int keep = std::min(nconv + l, m - 1);
+        if (p->prof) KORE_TRY(kore_prof_mark(p, 4, true));
         k_gemm_vg<<<c.grid, 256, 0, p->stream>>>(np, m, keep, c.V, dQ, m, c.Vtmp);
         KORE_CUDA_TRY(cudaMemcpyAsync(c.Vtmp + (int64_t)keep * np, c.V + (int64_t)m * np, np * sizeof(double2),
                                       cudaMemcpyDeviceToDevice, p->stream));
         k_restart_h<<<1, 256, 0, p->stream>>>(m, keep, dT, dbnew, c.Hbar);
         KORE_LAUNCHED(2);
+        if (p->prof) KORE_TRY(kore_prof_mark(p, 4, false));
         std::swap(c.V, c.Vtmp);
         kkeep = keep;
     }
@@ -626,7 +668,7 @@ int kore_eigs_impl(kore_plan *p, const kore_eps_opts *o, double *evals, double *
         for (int j = 0; j < nout; ++j) {
             double2 *x = c.Vtmp + (int64_t)j * np;
             if (o->purify) {
-                KORE_TRY(apply_op(c, x, c.w, st, &iters_max, &res_max));
+                KORE_TRY(apply_op(c, x, c.w));
                 KORE_CUDA_TRY(cudaMemcpyAsync(x, c.w, np * sizeof(double2), cudaMemcpyDeviceToDevice, p->stream));
             }
             k_nrm2_partial<<<c.grid, 256, 0, p->stream>>>(np, x, c.dpart);
@@ -641,11 +683,16 @@ int kore_eigs_impl(kore_plan *p, const kore_eps_opts *o, double *evals, double *
     KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
     KORE_TRY(kore_check_device_error(p));
     *nconv_out = nconv;
+    IrState irs;
+    KORE_TRY(kore_ir_read(p, &irs));
+    if (irs.nan) return KORE_ENAN;
     if (st) {
         st->nconv = nconv;
         st->restarts = restarts + 1;
-        st->refine_iters_max = iters_max;
-        st->solve_resid_max = res_max;
+        st->op_applies = (p->prec == KORE_PREC_MIXED) ? irs.applies : irs.sweeps;
+        st->sweeps = irs.sweeps;
+        st->refine_iters_max = irs.iters_max;
+        st->solve_resid_max = irs.eta_max;
         st->iterate_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     return nconv > 0 ? KORE_OK : KORE_ENOCONV;

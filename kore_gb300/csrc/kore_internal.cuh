@@ -4,6 +4,22 @@
 #include <vector>
 #include "kore_common.cuh"
 
+// Device-side state of the FP64 refinement loop and solve counters.
+struct IrState {
+    int done;          // current refinement finished
+    int nan;           // a residual was NaN/Inf
+    int iters;         // corrections applied (total)
+    int iters_cur;     // corrections of the current application
+    int iters_max;     // worst corrections of one application
+    int applies;       // applications of the inverse
+    int sweeps;        // sweeps that ran
+    int pad_;
+    double prev;       // previous eta of the current application
+    double eta_max;    // worst final eta
+    int sweeps_total;  // sweeps that ran since the plan was created (kept by kore_ir_reset)
+    int pad2_;
+};
+
 // One level of the block cyclic reduction.  Couplings of levels >= 1 are dense S x S
 // blocks in kore_plan::d_LU: L of position q at lu_L + q, U at lu_U + q (block units).
 struct BcrLevel {
@@ -64,10 +80,12 @@ struct kore_plan {
     // solve workspace (padded, complex128 unless noted)
     double2 *d_v[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     void *d_zlo = nullptr, *d_xlo = nullptr, *d_flo = nullptr;   // sweep vectors in factor precision
-    double *d_red = nullptr;          // reduction scratch (4096 doubles)
+    double *d_red = nullptr;          // reduction scratch (8192 doubles)
+    double *d_part = nullptr;         // per-CTA maxima of the residual kernel (2 per CTA)
     double *h_red = nullptr;          // pinned host mirror
     int *d_err = nullptr;
     unsigned *d_bar = nullptr;
+    IrState *d_ir = nullptr;
 
     // Krylov-Schur workspace
     double2 *d_V = nullptr;           // np x (ncv+1)
@@ -84,9 +102,12 @@ struct kore_plan {
     bool prof = false;
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
-    std::vector<std::pair<int, size_t>> ev_marks;   // (kind 0 = sweep, 1 = factor, index of start event)
-    double prof_ms[2] = {0, 0};
-    long long prof_n[2] = {0, 0};
+    std::vector<std::pair<int, size_t>> ev_marks;   // (kind, index of the start event)
+    // kinds: 0 sweep, 1 factorisation, 2 sparse products (B x, residuals), 3 Krylov
+    // orthogonalisation, 4 projected Schur problem and restart
+    double prof_ms[5] = {0, 0, 0, 0, 0};
+    long long prof_n[5] = {0, 0, 0, 0, 0};
+    int sweeps_at_enable = 0;
 };
 
 // record a start (begin = true) or stop event of a timed region of `kind`
@@ -103,9 +124,10 @@ int kore_factor_impl(kore_plan *p, double sre, double sim, int precision);
 
 // sweep.cu
 // x = (A - sigma B)^-1 b on padded l-major complex128 vectors (device), refined in
-// FP64 when the factors are complex64.  Returns the refinement count in *iters.
-int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol, int *iters,
-                       double *resid);
+// FP64 when the factors are complex64 (asynchronous; counters in the plan's IrState).
+int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol);
+int kore_ir_reset(kore_plan *p);
+int kore_ir_read(kore_plan *p, IrState *out);
 // y = B x on padded vectors
 int kore_spmv_b(kore_plan *p, const double2 *x, double2 *y);
 // y = A x - lam B x on padded vectors

@@ -95,7 +95,7 @@ void free_plan(kore_plan *p) {
     void *ptrs[] = {p->d_arow, p->d_acol, p->d_asplit, p->d_aval, p->d_brow, p->d_bcol, p->d_bval,
                     p->d_slot2orig, p->d_bsz, p->d_Dinv, p->d_Gm, p->d_Hm, p->d_Dw, p->d_LU, p->d_lev,
                     p->d_rscale, p->d_T, p->d_piv, p->d_pidx, p->d_used, p->d_zlo, p->d_xlo, p->d_flo,
-                    p->d_red, p->d_err, p->d_bar, p->d_V, p->d_Vtmp, p->d_small};
+                    p->d_red, p->d_part, p->d_err, p->d_bar, p->d_ir, p->d_V, p->d_Vtmp, p->d_small};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     for (auto &v : p->d_v)
@@ -223,8 +223,12 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
     KORE_TRY(kore_alloc(p, (void **)&p->d_used, (size_t)p->nodd_max * p->S * sizeof(int)));
     for (auto &v : p->d_v) KORE_TRY(kore_alloc(p, (void **)&v, p->np * sizeof(double2)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_red, 8192 * sizeof(double)));
+    // one pair of maxima per CTA of the residual kernel (16 lanes per row, 256 threads)
+    KORE_TRY(kore_alloc(p, (void **)&p->d_part, 2 * (size_t)kore_div_up(p->np * 16, 256) * sizeof(double)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_err, sizeof(int)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_bar, 64));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_ir, sizeof(IrState)));
+    KORE_CUDA_TRY(cudaMemset(p->d_ir, 0, sizeof(IrState)));
     KORE_CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
     KORE_CUDA_TRY(cudaMemset(p->d_piv, 0, (size_t)p->nodd_max * p->S * sizeof(int)));
     KORE_CUDA_TRY(cudaMemset(p->d_pidx, 0xff, (size_t)p->nodd_max * p->S * sizeof(int)));
@@ -237,17 +241,19 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
 }
 
 int solve_dev_impl(kore_plan *p, const double2 *b, double2 *x, int nrhs, double tol, kore_stats *st) {
+    KORE_TRY(kore_ir_reset(p));
     for (int k = 0; k < nrhs; ++k) {
         KORE_TRY(kore_gather(p, b + (int64_t)k * p->n, p->d_v[0]));
-        int it = 0;
-        double res = 0.0;
-        KORE_TRY(kore_apply_inverse(p, p->d_v[0], p->d_v[1], tol, &it, &res));
+        KORE_TRY(kore_apply_inverse(p, p->d_v[0], p->d_v[1], tol));
         KORE_TRY(kore_scatter(p, p->d_v[1], x + (int64_t)k * p->n));
-        if (st) {
-            st->sweeps += std::max(it, 1);
-            st->refine_iters_max = std::max(st->refine_iters_max, it);
-            st->solve_resid_max = std::max(st->solve_resid_max, res);
-        }
+    }
+    if (st) {
+        IrState s;
+        KORE_TRY(kore_ir_read(p, &s));
+        st->sweeps = s.sweeps;
+        st->refine_iters_max = s.iters_max;
+        st->solve_resid_max = s.eta_max;
+        if (s.nan) return KORE_ENAN;
     }
     return KORE_OK;
 }
@@ -342,11 +348,15 @@ int kore_profile(kore_plan *p, int enable, double *out) {
     if (!p) return KORE_EINVAL;
     DeviceGuard g(p->device);
     KORE_TRY(kore_prof_collect(p));
+    IrState irs;
+    KORE_TRY(kore_ir_read(p, &irs));
     if (out) {
         const double e = p->factor_elt ? (double)p->factor_elt : 16.0;
         const double S = p->S, K = p->K, np = (double)p->np;
         out[0] = p->prof_ms[0];
-        out[1] = (double)p->prof_n[0];
+        // sweeps that ran (sweep launches that returned at once, after the refinement
+        // converged, are excluded: their events enclose no work)
+        out[1] = (double)(irs.sweeps_total - p->sweeps_at_enable);
         out[2] = p->prof_ms[1];
         out[3] = (double)p->prof_n[1];
         // one sweep reads every D^-1, G, H block once, the dense couplings of the even
@@ -366,10 +376,14 @@ int kore_profile(kore_plan *p, int enable, double *out) {
             if (l > 0) gm += 4.0 * p->lev[l].neven;
         }
         out[5] = (gj + 1.0) * 28.0 * S * S * S + gm * 8.0 * S * S * S;
+        for (int k = 2; k < 5; ++k) {
+            out[6 + 2 * (k - 2)] = p->prof_ms[k];
+            out[7 + 2 * (k - 2)] = (double)p->prof_n[k];
+        }
     }
     if (enable) {
-        p->prof_ms[0] = p->prof_ms[1] = 0.0;
-        p->prof_n[0] = p->prof_n[1] = 0;
+        for (int k = 0; k < 5; ++k) { p->prof_ms[k] = 0.0; p->prof_n[k] = 0; }
+        p->sweeps_at_enable = irs.sweeps_total;
     }
     p->prof = enable != 0;
     return KORE_OK;
