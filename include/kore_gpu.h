@@ -130,6 +130,27 @@ int kore_solve_dev(kore_plan *plan, const void *b_dev, void *x_dev, int nrhs,
                    double refine_tol, void *stream, kore_stats *stats);
 
 /*
+ * x = (A - sigma B)^-1 b for one right-hand side, like kore_solve_dev, but without
+ * allocating anything: no cudaMalloc/cudaFree and no allocating library routine.
+ * This entry point has no counterpart in the reference; it is for callers that
+ * cannot allocate device memory when they solve (a fixed memory budget or a pool they
+ * do not own, a latency-critical loop that must not take the device-wide
+ * synchronisation of cudaMalloc/cudaFree, a host library handed only a stream).
+ * Its scratch is one file-scope device array of fixed size held by every GPU that
+ * loads the library until exit; problems with more than 16384 padded unknowns
+ * (blocks x largest block size) are rejected with KORE_EINVAL and a message on
+ * stderr.  b_dev and x_dev are complex128 device vectors in the original unknown
+ * order; the kernels run on `stream` (0 = the legacy default stream) of the plan's
+ * device and the call returns after they finish.  The first call on a device looks
+ * up the scratch address (set-up); make that first call before any stream capture.
+ * Every call shares the one scratch array and keeps the last call's contents, so
+ * calls whose work overlaps on the GPU (other threads, other streams) race: serialise
+ * them.
+ */
+int kore_solve_dev_noalloc(kore_plan *plan, const void *b_dev, void *x_dev, double refine_tol,
+                           void *stream);
+
+/*
  * Shift-and-invert Krylov-Schur for A x = lambda B x around the factorised shift.
  * Replaces E.solve() and the getEigenpair loop (bin/solve.py:123-158).  evals
  * receives up to ncv complex eigenvalues in SLEPc order (converged first, sorted by

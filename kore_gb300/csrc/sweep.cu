@@ -16,6 +16,7 @@
 //     r = b - (A - sigma B) x,  x += M32^-1 r   until ||r||_inf <= tol (||M||_inf ||x||_inf + ||b||_inf).
 #include "kore_internal.cuh"
 #include <cstddef>
+#include <mutex>
 
 namespace {
 
@@ -502,4 +503,157 @@ int kore_ir_read(kore_plan *p, IrState *out) {
     KORE_CUDA_TRY(cudaMemcpyAsync(out, p->d_ir, sizeof(IrState), cudaMemcpyDeviceToHost, p->stream));
     KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
     return KORE_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Allocation-free solve: kore_solve_dev_noalloc (include/kore_gpu.h).
+//
+// Some callers cannot allocate device memory at the moment they need a solve: code
+// that runs under a fixed memory budget or a pool it does not own, code that must not
+// trigger the implicit device synchronisation of cudaMalloc/cudaFree inside a
+// latency-critical loop, or a host library that is handed only a stream.  For them the
+// scratch of one solve (padded right-hand side and solution, the reduction vectors of
+// the sweep, the FP64 residual and the per-CTA maxima of the refinement loop, the
+// grid-barrier counter, the error flag and the refinement state) lives in the
+// file-scope array below instead of in buffers of the plan or of a caller.  Its size
+// is fixed at kNoAllocMaxNp padded unknowns (about 1.6 MB, held by every GPU that
+// loads the library until the process exits); larger problems are rejected.
+// The kernels are the ones of kore_solve_dev; only their scratch pointers differ.
+namespace {
+
+constexpr int64_t kNoAllocMaxNp = 16384;
+constexpr int64_t kNoAllocMaxSpmvCta = (kNoAllocMaxNp * kRowLanes + 255) / 256;
+
+struct NoAllocScratch {
+    double2 bp[kNoAllocMaxNp];      // padded right-hand side (complex128)
+    double2 xp[kNoAllocMaxNp];      // padded solution
+    double2 r[kNoAllocMaxNp];       // FP64 residual of the refinement loop
+    double2 f[kNoAllocMaxNp];       // sweep reduction vectors, room for complex128
+    double2 z[kNoAllocMaxNp];
+    double2 x[kNoAllocMaxNp];
+    double part[2 * kNoAllocMaxSpmvCta];   // per-CTA maxima of the residual kernel
+    double red[2048 + 8];                  // ||b||_inf partials [0, 2048), then scalars
+    IrState ir;
+    unsigned bar[16];
+    int err;
+};
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// Device address of g_noalloc_scratch, looked up once per device (the symbol's name
+// in host code is only a stand-in and must never be passed to a kernel).
+std::mutex g_noalloc_mu;
+NoAllocScratch *g_noalloc_addr[64] = {};
+
+int noalloc_scratch(int device, NoAllocScratch **out) {
+    if (device < 0 || device >= 64) return KORE_EINVAL;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void *ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr) {
+            std::fprintf(stderr, "kore: cudaGetSymbolAddress of the no-allocation scratch failed: %s\n",
+                         cudaGetErrorString(e));
+            return KORE_ECUDA;
+        }
+        g_noalloc_addr[device] = static_cast<NoAllocScratch *>(ptr);
+    }
+    *out = g_noalloc_addr[device];
+    return KORE_OK;
+}
+
+template <typename C>
+int noalloc_sweep(kore_plan *p, NoAllocScratch *s, const double2 *b, const double *bnorm, double2 *x, int accumulate,
+                  const int *skip, cudaStream_t st) {
+    SweepArgs a;
+    a.K = p->K; a.S = p->S; a.nlev = p->nlev; a.levs = p->d_lev;
+    a.Dinv = p->d_Dinv; a.G = p->d_Gm; a.H = p->d_Hm; a.LU = p->d_LU;
+    a.arow = p->d_arow; a.acol = p->d_acol; a.asplit = p->d_asplit; a.aval = p->d_aval;
+    a.b = b; a.rscale = p->d_rscale; a.bnorm = bnorm;
+    a.f = s->f; a.z = s->z; a.x = s->x;
+    a.out = x; a.accumulate = accumulate; a.bar = s->bar; a.err = &s->err;
+    a.skip = skip; a.count = &s->ir.sweeps; a.count_total = &s->ir.sweeps_total;
+    const size_t smem = 2 * (size_t)p->S * sizeof(C);
+    auto kern = k_sweep<C>;
+    if (smem > 48 * 1024)
+        KORE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    KORE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kSweepThreads, smem));
+    occ = std::max(1, std::min(occ, 4));
+    KORE_CUDA_TRY(cudaMemsetAsync(s->bar, 0, sizeof(unsigned), st));
+    void *args[] = {&a};
+    dim3 grid(p->num_sms * occ), block(kSweepThreads);
+    KORE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)kern, grid, block, args, smem, st));
+    KORE_LAUNCHED(1);
+    return KORE_OK;
+}
+
+int noalloc_solve(kore_plan *p, NoAllocScratch *s, const double2 *b_dev, double2 *x_dev, double tol, cudaStream_t st) {
+    const bool mixed = p->prec == KORE_PREC_MIXED;
+    const unsigned g = std::min<unsigned>(kore_div_up(p->np, 256), 1024u);
+    double *bn = s->red + 2048, *rn = s->red + 2049;
+    // every call starts from a cleared error flag and refinement state
+    KORE_CUDA_TRY(cudaMemsetAsync(&s->err, 0, sizeof(int), st));
+    KORE_CUDA_TRY(cudaMemsetAsync(&s->ir, 0, sizeof(IrState), st));
+    k_gather<<<std::min<unsigned>(kore_div_up(p->np, 256), 2048u), 256, 0, st>>>(p->np, p->d_slot2orig, b_dev, s->bp);
+    k_absmax<<<g, 256, 0, st>>>(p->np, s->bp, s->red);
+    k_reduce_max<<<1, 1024, 0, st>>>(s->red, (int)g, bn);
+    KORE_LAUNCHED(3);
+    if (!mixed) {
+        KORE_TRY(noalloc_sweep<double2>(p, s, s->bp, bn, s->xp, 0, nullptr, st));
+    } else {
+        if (!(tol > 0.0)) tol = 1e-14;
+        k_ir_begin<<<1, 1, 0, st>>>(&s->ir);
+        KORE_LAUNCHED(1);
+        KORE_TRY(noalloc_sweep<float2>(p, s, s->bp, bn, s->xp, 0, nullptr, st));
+        const unsigned grid = kore_div_up(p->np * kRowLanes, 256);
+        for (int it = 0; it < kIrMax; ++it) {
+            k_spmv<<<grid, 256, 0, st>>>(p->np, 2, p->d_arow, p->d_acol, p->d_aval, p->d_brow, p->d_bcol, p->d_bval,
+                                         p->has_b ? 1 : 0, p->sigma_re, p->sigma_im, s->xp, s->bp, s->r, s->part,
+                                         &s->ir.done);
+            k_ir_check<<<1, 1024, 0, st>>>(s->part, (int)grid, bn, p->minf, tol, &s->ir, rn);
+            KORE_LAUNCHED(2);
+            KORE_TRY(noalloc_sweep<float2>(p, s, s->r, rn, s->xp, 1, &s->ir.done, st));
+        }
+    }
+    k_scatter<<<std::min<unsigned>(kore_div_up(p->np, 256), 2048u), 256, 0, st>>>(p->np, p->d_slot2orig, s->xp, x_dev);
+    KORE_LAUNCHED(1);
+    KORE_CUDA_TRY(cudaGetLastError());
+    return KORE_OK;
+}
+
+}  // namespace
+
+extern "C" int kore_solve_dev_noalloc(kore_plan *p, const void *b_dev, void *x_dev, double refine_tol, void *stream) {
+    if (!p || !b_dev || !x_dev) return KORE_EINVAL;
+    if (p->np > kNoAllocMaxNp) {
+        std::fprintf(stderr,
+                     "kore_solve_dev_noalloc: %lld padded unknowns exceed the fixed scratch of %lld; "
+                     "use kore_solve_dev\n",
+                     (long long)p->np, (long long)kNoAllocMaxNp);
+        return KORE_EINVAL;
+    }
+    if (!p->factored) return KORE_ENOTFACTORED;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != p->device) KORE_CUDA_TRY(cudaSetDevice(p->device));
+    NoAllocScratch *s = nullptr;
+    int rc = noalloc_scratch(p->device, &s);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (rc == KORE_OK) rc = noalloc_solve(p, s, static_cast<const double2 *>(b_dev), static_cast<double2 *>(x_dev),
+                                          refine_tol, st);
+    if (rc == KORE_OK) {
+        // wait for this call's kernels, then read its error flag and NaN state
+        int flags[2] = {0, 0};
+        if (cudaMemcpyAsync(&flags[0], &s->err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(&flags[1], &s->ir.nan, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            rc = KORE_ECUDA;
+        else if (flags[0] != 0)
+            rc = KORE_ETIMEOUT;
+        else if (flags[1] != 0)
+            rc = KORE_ENAN;
+    }
+    if (prev >= 0 && prev != p->device) cudaSetDevice(prev);
+    return rc;
 }
