@@ -1,0 +1,48 @@
+"""The host restatement of the hydrodynamic assembly (kore_gb300.assembly) against
+the pencils the reference's own submatrices.py/assemble.py produced."""
+import numpy as np
+import pytest
+import scipy.sparse.linalg as ssl
+
+from kore_gb300.assembly import chebco, hydro_pencil, mult_mat, ncheb
+
+HYDRO = ["spinover", "shell_m1_ek1e-4", "shell_m2_small", "shell_m2_ek1e-4", "forced_m2_f10", "forced_m2_f7"]
+
+
+@pytest.mark.parametrize("name", HYDRO)
+def test_matches_reference_assembly(case, name):
+    meta, A, B = case(name)
+    A2, B2 = hydro_pencil(meta["m"], meta["symm"], meta["Ek"], meta["N"], meta["lmax"], meta["ricb"],
+                          forcing=meta["forcing"], forcing_frequency=meta["forcing_frequency"])
+    assert A2.shape == A.shape and B2.shape == B.shape
+    assert ssl.norm(A2 - A) <= 1e-14 * ssl.norm(A)
+    assert ssl.norm(B2 - B) <= 1e-14 * ssl.norm(B)
+    # entrywise, relative to the largest entry of the row
+    D = abs(A2 - A).tocsr()
+    rowmax = np.asarray(abs(A).max(axis=1).todense()).ravel()
+    assert (D.multiply(1.0 / np.maximum(rowmax, 1e-300)[:, None])).max() < 1e-13
+
+
+def test_chebyshev_coefficients_of_powers():
+    # r^2 on [0.35, 1] has exactly three nonzero Chebyshev coefficients
+    c = chebco(2, 16, 1e-9, 0.35)
+    assert np.count_nonzero(c) == 3
+    x = 0.3
+    r = 0.35 + 0.65 * (x + 1) / 2
+    assert abs(np.polynomial.chebyshev.chebval(x, c) - r * r) < 1e-14
+
+
+def test_multiplication_operator_lambda0_is_chebyshev_product():
+    a = chebco(1, 12, 1e-12, 0.35)
+    b = np.zeros(12)
+    b[:5] = [0.3, -0.2, 0.1, 0.05, 0.01]
+    prod = mult_mat(a, 0) @ b
+    full = np.polynomial.chebyshev.chebmul(a, b)
+    ref = np.zeros(12)
+    ref[:min(12, full.size)] = full[:12]
+    assert np.abs(prod - ref).max() < 1e-14
+
+
+def test_ncheb_rule():
+    # bin/parameters.py:6-16
+    assert ncheb(1e-3) == 68 and ncheb(1e-7) == 428 and ncheb(0) == 48

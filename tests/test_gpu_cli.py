@@ -1,0 +1,74 @@
+"""The drop-in solve.py run like the reference's own end-to-end tests
+(tests/test_spinover.py: solve in a case directory, read eigenvalues0.dat, compare the
+max-Re eigenvalue with reference.eig at rtol 1e-8)."""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from oracle.eps_ref import forced_solve
+
+pytestmark = pytest.mark.gpu
+
+SPINOVER_GOLDEN = np.array([-1.019947097016500742e-01, 1.005733690103750355e+00])
+
+
+def write_case(tmp, meta, A, B):
+    os.makedirs(os.path.join(tmp, "bin"), exist_ok=True)
+    tau = complex(*meta["tau"])
+    lines = [f"{k} = {meta[k]!r}" for k in ("hydro", "magnetic", "thermal", "compositional", "m", "symm", "ricb",
+                                            "N", "lmax", "forcing", "nev", "tol", "maxit", "which_eigenpairs", "B0")]
+    lines.append(f"tau = complex({tau.real!r}, {tau.imag!r})")
+    lines.append("B0_l = 1")
+    with open(os.path.join(tmp, "bin", "parameters.py"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    np.savez(os.path.join(tmp, "A.npz"), data=A.data, indices=A.indices, indptr=A.indptr, shape=A.shape)
+    name = "B.npz" if meta["forcing"] == 0 else "B_forced.npz"
+    np.savez(os.path.join(tmp, name), data=B.data, indices=B.indices, indptr=B.indptr, shape=B.shape)
+
+
+def run_cli(tmp, *args):
+    cmd = [sys.executable, os.path.join(ROOT, "kore_gb300", "cli", "solve.py")] + list(args)
+    r = subprocess.run(cmd, cwd=tmp, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return r.stdout
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cli_spinover(gpu_lib, case, tmp_path, precision):
+    meta, A, B = case("spinover")
+    write_case(str(tmp_path), meta, A, B)
+    out = run_cli(str(tmp_path), "-st_type", "sinvert", "-eps_error_relative", "::ascii_info_detail",
+                  "-kore_precision", precision)
+    assert "Solve done in" in out
+    dat = np.loadtxt(tmp_path / "eigenvalues0.dat")
+    i = np.argmax(dat[:, 0])
+    np.testing.assert_allclose(dat[i, :], SPINOVER_GOLDEN, rtol=1e-8, atol=1e-20)
+    n = meta["sizmat"] // 2
+    rf = np.loadtxt(tmp_path / "real_flow.field")
+    imf = np.loadtxt(tmp_path / "imag_flow.field")
+    assert rf.shape == (2 * n, dat.shape[0]) and imf.shape == rf.shape
+    # unit-norm eigenvectors satisfy A x = lambda B x
+    lam = dat[:, 0] + 1j * dat[:, 1]
+    X = rf + 1j * imf
+    for k in range(len(lam)):
+        x = X[:, k]
+        assert abs(np.linalg.norm(x) - 1.0) < 1e-10
+        assert np.linalg.norm(A @ x - lam[k] * (B @ x)) < 1e-9 * (abs(lam[k]) + 1)
+    assert os.path.exists(tmp_path / "timing.dat")
+
+
+def test_cli_forced(gpu_lib, case, tmp_path):
+    meta, A, bf = case("forced_m2_f10")
+    write_case(str(tmp_path), meta, A, bf)
+    out = run_cli(str(tmp_path), "-ksp_type", "preonly", "-pc_type", "lu", "-kore_precision", "fp64")
+    assert "Solution(s) computed" in out
+    x = np.loadtxt(tmp_path / "real_flow.field") + 1j * np.loadtxt(tmp_path / "imag_flow.field")
+    ref = forced_solve(A, bf.toarray().ravel())
+    assert x.shape == ref.shape
+    assert np.linalg.norm(x - ref) / np.linalg.norm(ref) < 1e-9
+
+
