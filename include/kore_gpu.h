@@ -119,10 +119,20 @@ int kore_plan_create(const kore_pencil_desc *desc, int device, kore_plan **plan)
 int kore_factor(kore_plan *plan, double sigma_re, double sigma_im, int precision);
 
 /*
+ * Factorises A - sigma_s B for nshift shifts at once (sigmas: nshift interleaved
+ * re, im pairs), e.g. the forcing frequencies sigma = i*omega of a batch of forced
+ * problems on one eigen pencil (bin/assemble.py makes the forced matrix
+ * ||u||_F (A_eig - i omega B_eig)).  Every kernel of the factorisation and of the
+ * solves covers all shifts in one launch.  kore_factor is the nshift = 1 case.
+ */
+int kore_factor_shifts(kore_plan *plan, int nshift, const double *sigmas, int precision);
+
+/*
  * x = (A - sigma B)^-1 b for nrhs right-hand sides stored one after another
- * (column k at b + 2*n*k).  Replaces K.solve(bvec, x) (bin/solve.py:227).  In mixed
- * precision the result is refined in FP64 to relative residual <= refine_tol
- * (refine_tol <= 0 selects 1e-14).
+ * (column k at b + 2*n*k); with several factorised shifts nrhs must be a multiple of
+ * nshift and right-hand side k is solved with shift k % nshift.  Replaces
+ * K.solve(bvec, x) (bin/solve.py:227).  In mixed precision the result is refined in
+ * FP64 to relative residual <= refine_tol (refine_tol <= 0 selects 1e-14).
  */
 int kore_solve(kore_plan *plan, const double *b, double *x, int nrhs, double refine_tol,
                kore_stats *stats);
@@ -151,7 +161,8 @@ int kore_solve_dev_noalloc(kore_plan *plan, const void *b_dev, void *x_dev, doub
                            void *stream);
 
 /*
- * Shift-and-invert Krylov-Schur for A x = lambda B x around the factorised shift.
+ * Shift-and-invert Krylov-Schur for A x = lambda B x around the factorised shift
+ * (one shift: KORE_EINVAL after kore_factor_shifts with nshift > 1).
  * Replaces E.solve() and the getEigenpair loop (bin/solve.py:123-158).  evals
  * receives up to ncv complex eigenvalues in SLEPc order (converged first, sorted by
  * `which`), evecs (may be NULL) up to ncv unit-2-norm eigenvectors in the original

@@ -20,7 +20,7 @@ PREC = {"fp64": 0, "mixed": 1}
 WHICH = {"LM": 0, "SM": 1, "LR": 2, "SR": 3, "LI": 4, "SI": 5, "TM": 6, "TR": 7, "TI": 8}
 
 # every function include/kore_gpu.h declares
-EXPORTS = ("kore_plan_create", "kore_factor", "kore_solve", "kore_solve_dev", "kore_solve_dev_noalloc", "kore_eigs",
+EXPORTS = ("kore_plan_create", "kore_factor", "kore_factor_shifts", "kore_solve", "kore_solve_dev", "kore_solve_dev_noalloc", "kore_eigs",
            "kore_residual", "kore_plan_stream", "kore_profile", "kore_plan_bytes", "kore_kernel_launches",
            "kore_status_string", "kore_plan_destroy")
 
@@ -91,6 +91,7 @@ def _bind(lib):
     P = C.c_void_p
     lib.kore_plan_create.argtypes = [C.POINTER(PencilDesc), C.c_int, C.POINTER(P)]
     lib.kore_factor.argtypes = [P, C.c_double, C.c_double, C.c_int]
+    lib.kore_factor_shifts.argtypes = [P, C.c_int, P, C.c_int]
     lib.kore_solve.argtypes = [P, P, P, C.c_int, C.c_double, C.POINTER(Stats)]
     lib.kore_solve_dev.argtypes = [P, P, P, C.c_int, C.c_double, P, C.POINTER(Stats)]
     lib.kore_solve_dev_noalloc.argtypes = [P, P, P, C.c_double, P]

@@ -27,6 +27,10 @@
 // never swapped: the pivot row of column k is recorded and the outputs are gathered
 // by it.  Pivoting stays inside each diagonal block.
 //
+// Many shifts (forcing frequencies, targets) of one pencil are factorised together:
+// every kernel carries the shift as one more grid dimension, and shift s uses its own
+// row scales and factor set at offset s * stride.
+//
 // This replaces the sparse LU that SLEPc's ST sinvert / PETSc's PCLU build inside
 // bin/solve.py:123 and :227; the ordering (odd-even elimination of l-blocks) is what
 // exposes the parallelism.
@@ -36,26 +40,60 @@
 
 namespace {
 
+// Device view of the plan for the factorisation kernels; shift s uses offset
+// s * (f|lu|t|p|rs)_stride into the per-shift buffers.
+template <typename C>
+struct FV {
+    int S, K;
+    int64_t np;
+    const int *arow, *acol, *asplit, *brow, *bcol, *bsz;
+    const double2 *aval;
+    const double *bval;
+    int has_b;
+    const double2 *sigma;
+    double *rscale;
+    C *Dinv, *G, *H, *Dw, *LU, *T;
+    int *piv, *pidx, *used, *err;
+    int64_t f_stride, lu_stride, t_stride, p_stride;
+};
+
+template <typename C>
+FV<C> make_fv(kore_plan *p) {
+    FV<C> v;
+    v.S = p->S; v.K = p->K; v.np = p->np;
+    v.arow = p->d_arow; v.acol = p->d_acol; v.asplit = p->d_asplit; v.brow = p->d_brow; v.bcol = p->d_bcol;
+    v.bsz = p->d_bsz; v.aval = p->d_aval; v.bval = p->d_bval; v.has_b = p->has_b ? 1 : 0;
+    v.sigma = p->d_sigma; v.rscale = p->d_rscale;
+    v.Dinv = static_cast<C *>(p->d_Dinv); v.G = static_cast<C *>(p->d_Gm); v.H = static_cast<C *>(p->d_Hm);
+    v.Dw = static_cast<C *>(p->d_Dw); v.LU = static_cast<C *>(p->d_LU); v.T = static_cast<C *>(p->d_T);
+    v.piv = p->d_piv; v.pidx = p->d_pidx; v.used = p->d_used; v.err = p->d_err;
+    v.f_stride = p->f_stride(); v.lu_stride = p->lu_stride(); v.t_stride = p->t_stride(); v.p_stride = p->p_stride();
+    return v;
+}
+
 // Row equilibration by powers of two (exact): rscale[p] = 2^-e with
 // e = exponent of max(max_e |a_pe|, |sigma| max_e |b_pe|); also the row 1-norms of
-// |A| + |sigma||B| whose maximum bounds ||A - sigma B||_inf.
-__global__ void k_rowinfo(int64_t np, const int *__restrict__ arow, const double2 *__restrict__ aval,
-                          const int *__restrict__ brow, const double *__restrict__ bval, int has_b,
-                          double sabs, double *__restrict__ rscale, double *__restrict__ red) {
+// |A| + |sigma||B| whose maximum bounds ||A - sigma B||_inf.  Shift = blockIdx.y;
+// per-CTA maxima to red[s * gridDim.x + blockIdx.x].
+template <typename C>
+__global__ void k_rowinfo(FV<C> v, double *__restrict__ red) {
+    const int s = blockIdx.y;
+    const double2 sg = v.sigma[s];
+    const double sabs = sqrt(abs2(sg));
+    double *rscale = v.rscale + (int64_t)s * v.np;
     double mx = 0.0;
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
-         p += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < v.np; p += (int64_t)gridDim.x * blockDim.x) {
         double am = 0.0, sum = 0.0;
-        for (int e = arow[p]; e < arow[p + 1]; ++e) {
-            const double v = sqrt(abs2(aval[e]));
-            am = fmax(am, v);
-            sum += v;
+        for (int e = v.arow[p]; e < v.arow[p + 1]; ++e) {
+            const double t = sqrt(abs2(v.aval[e]));
+            am = fmax(am, t);
+            sum += t;
         }
-        if (has_b)
-            for (int e = brow[p]; e < brow[p + 1]; ++e) {
-                const double v = sabs * fabs(bval[e]);
-                am = fmax(am, v);
-                sum += v;
+        if (v.has_b)
+            for (int e = v.brow[p]; e < v.brow[p + 1]; ++e) {
+                const double t = sabs * fabs(v.bval[e]);
+                am = fmax(am, t);
+                sum += t;
             }
         rscale[p] = (am > 0.0) ? ldexp(1.0, -ilogb(am)) : 1.0;
         mx = fmax(mx, sum);
@@ -65,113 +103,113 @@ __global__ void k_rowinfo(int64_t np, const int *__restrict__ arow, const double
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = mx;
     __syncthreads();
     if (threadIdx.x < 32) {
-        double v = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
-        v = warp_max_d(v);
-        if (threadIdx.x == 0) red[blockIdx.x] = v;
+        double t = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+        t = warp_max_d(t);
+        if (threadIdx.x == 0) red[(int64_t)s * gridDim.x + blockIdx.x] = t;
     }
 }
 
-// Dw <- 0 with the identity on the padded diagonal of every block.
+// Dw <- 0 with the identity on the padded diagonal of every block, all shifts.
 template <typename C>
-__global__ void k_Dw_init(C *__restrict__ Dw, int K, int S, const int *__restrict__ bsz) {
-    const int64_t SS = (int64_t)S * S, total = (int64_t)K * SS;
+__global__ void k_Dw_init(FV<C> v, int nshift) {
+    const int64_t SS = (int64_t)v.S * v.S, per = (int64_t)v.K * SS, total = per * nshift;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
          idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = idx / SS;
-        const int64_t e = idx - i * SS;
-        const int c = (int)(e / S), r = (int)(e - (int64_t)c * S);
-        Dw[idx] = (r == c && r >= bsz[i]) ? cone<C>() : czero<C>();
+        const int64_t w = idx % per;
+        const int64_t i = w / SS;
+        const int64_t e = w - i * SS;
+        const int c = (int)(e / v.S), r = (int)(e - (int64_t)c * v.S);
+        v.Dw[idx] = (r == c && r >= v.bsz[i]) ? cone<C>() : czero<C>();
     }
 }
 
-// One warp per row: Dw_i[r, :] = rs_r (D_i - sigma B_i)[r, :] from the CSR.  A and B
-// entries of the same column are combined in FP64 and rounded once.
+// One warp per (shift, row): Dw_i[r, :] = rs_r (D_i - sigma B_i)[r, :] from the CSR.
+// A and B entries of the same column are combined in FP64 and rounded once.
 template <typename C>
-__global__ void k_Dw_scatter(C *__restrict__ Dw, int64_t np, int S, const int *__restrict__ arow,
-                             const int *__restrict__ acol, const double2 *__restrict__ aval,
-                             const int *__restrict__ asplit, const int *__restrict__ brow,
-                             const int *__restrict__ bcol, const double *__restrict__ bval, int has_b,
-                             double sre, double sim, const double *__restrict__ rscale) {
+__global__ void k_Dw_scatter(FV<C> v, int nshift) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const double2 sigma = mk(sre, sim);
-    for (int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; p < np; p += nw) {
+    const int S = v.S;
+    for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < v.np * nshift; w += nw) {
+        const int64_t s = w / v.np, p = w - s * v.np;
         const int64_t i = p / S;
         const int r = (int)(p - i * S);
-        const double rs = rscale[p];
-        C *D = Dw + i * (int64_t)S * S;
-        const int eD = asplit[2 * p], eU = asplit[2 * p + 1];
-        for (int e = eD + lane; e < eU; e += 32) D[r + (int64_t)(acol[e] - i * S) * S] = from_c128<C>(rs * aval[e]);
+        const double2 sigma = v.sigma[s];
+        const double rs = v.rscale[s * v.np + p];
+        C *D = v.Dw + s * v.f_stride + i * (int64_t)S * S;
+        const int eD = v.asplit[2 * p], eU = v.asplit[2 * p + 1];
+        for (int e = eD + lane; e < eU; e += 32) D[r + (int64_t)(v.acol[e] - i * S) * S] = from_c128<C>(rs * v.aval[e]);
         __syncwarp();
-        if (has_b)
-            for (int e = brow[p] + lane; e < brow[p + 1]; e += 32) {
-                const int c = bcol[e];
-                // matching A entry (binary search in the sorted D segment)
-                int lo = eD, hi = eU;
+        if (v.has_b)
+            for (int e = v.brow[p] + lane; e < v.brow[p + 1]; e += 32) {
+                const int c = v.bcol[e];
+                int lo = eD, hi = eU;   // matching A entry: binary search in the sorted D segment
                 while (lo < hi) {
                     const int mid = (lo + hi) >> 1;
-                    if (acol[mid] < c) lo = mid + 1; else hi = mid;
+                    if (v.acol[mid] < c) lo = mid + 1; else hi = mid;
                 }
-                const double2 a = (lo < eU && acol[lo] == c) ? aval[lo] : mk(0.0, 0.0);
-                D[r + (int64_t)(c - i * S) * S] = from_c128<C>(rs * (a - bval[e] * sigma));
+                const double2 a = (lo < eU && v.acol[lo] == c) ? v.aval[lo] : mk(0.0, 0.0);
+                D[r + (int64_t)(c - i * S) * S] = from_c128<C>(rs * (a - v.bval[e] * sigma));
             }
     }
 }
 
-// T_o = [Dw_j | L | U | I] for the odd blocks j of level lv; L, U copied from the
-// dense couplings (levels >= 1) or zeroed (level 0: scattered from the CSR next).
-// stride 0 selects block 0 (the top of the reduction).
+// T_o = [Dw_j | L | U | I] for the odd blocks j of level lv, all shifts; L, U copied
+// from the dense couplings (levels >= 1) or zeroed (level 0: scattered from the CSR
+// next).  stride 0 selects block 0 (the top of the reduction).
 template <typename C>
-__global__ void k_T_fill(C *__restrict__ T, const C *__restrict__ Dw, const C *__restrict__ LU, int S,
-                         BcrLevel lv, int nodd) {
-    const int64_t SS = (int64_t)S * S, per = 4 * SS, total = (int64_t)nodd * per;
+__global__ void k_T_fill(FV<C> v, BcrLevel lv, int nodd, int nshift) {
+    const int S = v.S;
+    const int64_t SS = (int64_t)S * S, per = 4 * SS, pershift = (int64_t)nodd * per, total = pershift * nshift;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
          idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t o = idx / per;
-        const int64_t e = idx - o * per;
+        const int64_t s = idx / pershift;
+        const int64_t ws = idx - s * pershift;
+        const int64_t o = ws / per;
+        const int64_t e = ws - o * per;
         const int part = (int)(e / SS);
         const int64_t w = e - (int64_t)part * SS;
         const int64_t q = 2 * o + 1;               // position of the odd block
         const int64_t j = q * lv.stride;           // original block
-        C v;
-        if (part == 0) v = Dw[j * SS + w];
+        C val;
+        if (part == 0) val = v.Dw[s * v.f_stride + j * SS + w];
         else if (part == 3) {
             const int c = (int)(w / S), r = (int)(w - (int64_t)c * S);
-            v = (r == c) ? cone<C>() : czero<C>();
-        } else if (lv.lu_L < 0) v = czero<C>();
-        else v = LU[((part == 1 ? lv.lu_L : lv.lu_U) + q) * SS + w];
-        T[idx] = v;
+            val = (r == c) ? cone<C>() : czero<C>();
+        } else if (lv.lu_L < 0) val = czero<C>();
+        else val = v.LU[s * v.lu_stride + ((part == 1 ? lv.lu_L : lv.lu_U) + q) * SS + w];
+        v.T[s * v.t_stride + o * per + e] = val;
     }
 }
 
-// Level 0: one warp per row of an odd block j: scatter rs * L_j and rs * U_j into T_o.
+// Level 0: one warp per (shift, row of an odd block j): scatter rs * L_j and rs * U_j into T_o.
 template <typename C>
-__global__ void k_T_scatter_LU(C *__restrict__ T, int S, int nodd, const int *__restrict__ arow,
-                               const int *__restrict__ acol, const double2 *__restrict__ aval,
-                               const int *__restrict__ asplit, const double *__restrict__ rscale) {
+__global__ void k_T_scatter_LU(FV<C> v, int nodd, int nshift) {
     const int lane = threadIdx.x & 31;
+    const int S = v.S;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t SS = (int64_t)S * S;
-    for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < (int64_t)nodd * S; w += nw) {
-        const int64_t o = w / S;
-        const int r = (int)(w - o * S);
+    const int64_t SS = (int64_t)S * S, rows = (int64_t)nodd * S;
+    for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < rows * nshift; w += nw) {
+        const int64_t s = w / rows, wr = w - s * rows;
+        const int64_t o = wr / S;
+        const int r = (int)(wr - o * S);
         const int64_t j = 2 * o + 1;
         const int64_t p = j * S + r;
-        const double rs = rscale[p];
-        C *To = T + o * 4 * SS;
-        for (int e = arow[p] + lane; e < asplit[2 * p]; e += 32)
-            To[r + (int64_t)(S + acol[e] - (j - 1) * S) * S] = from_c128<C>(rs * aval[e]);
-        for (int e = asplit[2 * p + 1] + lane; e < arow[p + 1]; e += 32)
-            To[r + (int64_t)(2 * S + acol[e] - (j + 1) * S) * S] = from_c128<C>(rs * aval[e]);
+        const double rs = v.rscale[s * v.np + p];
+        C *To = v.T + s * v.t_stride + o * 4 * SS;
+        for (int e = v.arow[p] + lane; e < v.asplit[2 * p]; e += 32)
+            To[r + (int64_t)(S + v.acol[e] - (j - 1) * S) * S] = from_c128<C>(rs * v.aval[e]);
+        for (int e = v.asplit[2 * p + 1] + lane; e < v.arow[p + 1]; e += 32)
+            To[r + (int64_t)(2 * S + v.acol[e] - (j + 1) * S) * S] = from_c128<C>(rs * v.aval[e]);
     }
 }
 
-// Panel reduction of columns [k0, k0+nb) of T_o, one CTA per odd block o.
+// Panel reduction of columns [k0, k0+nb) of T_o; one CTA per (odd block o = blockIdx.x,
+// shift = blockIdx.y).
 template <typename C, int NB>
-__global__ void __launch_bounds__(1024) k_panel(C *__restrict__ Tall, int S, int k0, int *__restrict__ pivall,
-                                                int *__restrict__ pidxall, int *__restrict__ usedall,
-                                                int *__restrict__ err) {
+__global__ void __launch_bounds__(1024) k_panel(FV<C> v, int k0) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int S = v.S;
     C *P = reinterpret_cast<C *>(smem_raw);
     int *u = reinterpret_cast<int *>(P + (size_t)S * NB);
     __shared__ C prow[NB];
@@ -180,9 +218,10 @@ __global__ void __launch_bounds__(1024) k_panel(C *__restrict__ Tall, int S, int
     __shared__ int s_p;
     __shared__ C s_dinv;
     __shared__ int s_piv[NB];
-    const int64_t o = blockIdx.x;
-    C *T = Tall + o * 4 * (int64_t)S * S;
-    int *piv = pivall + o * S, *pidx = pidxall + o * S, *used = usedall + o * S;
+    const int64_t o = blockIdx.x, sh = blockIdx.y;
+    C *T = v.T + sh * v.t_stride + o * 4 * (int64_t)S * S;
+    int *piv = v.piv + sh * v.p_stride + o * S, *pidx = v.pidx + sh * v.p_stride + o * S;
+    int *used = v.used + sh * v.p_stride + o * S;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int nb = min(NB, S - k0);
 
@@ -196,8 +235,8 @@ __global__ void __launch_bounds__(1024) k_panel(C *__restrict__ Tall, int S, int
         int bi = INT_MAX;
         for (int r = tid; r < S; r += nt)
             if (!u[r]) {
-                const double v = (double)abs2(P[c * S + r]);
-                if (v > best) { best = v; bi = r; }
+                const double val = (double)abs2(P[c * S + r]);
+                if (val > best) { best = val; bi = r; }
             }
         for (int off = 16; off > 0; off >>= 1) {
             const double ov = __shfl_down_sync(0xffffffffu, best, off);
@@ -218,7 +257,7 @@ __global__ void __launch_bounds__(1024) k_panel(C *__restrict__ Tall, int S, int
             if (tid == 0) {
                 int p = bi;
                 if (p >= S || !(best > 0.0)) {
-                    atomicCAS(err, 0, KORE_DEVERR_PIVOT);
+                    atomicCAS(v.err, 0, KORE_DEVERR_PIVOT);
                     p = -1;
                 } else {
                     u[p] = 1;
@@ -255,15 +294,14 @@ __global__ void __launch_bounds__(1024) k_panel(C *__restrict__ Tall, int S, int
     if (tid >= done && tid < nb) piv[k0 + tid] = 0;
 }
 
-// Trailing update of TW columns per CTA (blockIdx.x) of odd block blockIdx.y.
+// Trailing update of TW columns per CTA (blockIdx.x) of odd block blockIdx.y, shift blockIdx.z.
 template <typename C, int NB, int TW>
-__global__ void __launch_bounds__(256) k_update(C *__restrict__ Tall, int S, int k0, int nb, int col_begin,
-                                                int col_end, const int *__restrict__ pivall,
-                                                const int *__restrict__ pidxall) {
+__global__ void __launch_bounds__(256) k_update(FV<C> v, int k0, int nb, int col_begin, int col_end) {
     __shared__ C tp[TW][NB];
-    const int64_t o = blockIdx.y;
-    C *T = Tall + o * 4 * (int64_t)S * S;
-    const int *piv = pivall + o * S, *pidx = pidxall + o * S;
+    const int S = v.S;
+    const int64_t o = blockIdx.y, sh = blockIdx.z;
+    C *T = v.T + sh * v.t_stride + o * 4 * (int64_t)S * S;
+    const int *piv = v.piv + sh * v.p_stride + o * S, *pidx = v.pidx + sh * v.p_stride + o * S;
     const int j0 = col_begin + blockIdx.x * TW;
     const int tw = min(TW, col_end - j0);
     for (int idx = threadIdx.x; idx < TW * NB; idx += blockDim.x) {
@@ -288,62 +326,66 @@ __global__ void __launch_bounds__(256) k_update(C *__restrict__ Tall, int S, int
 }
 
 // Solution rows by pivot: Dinv_j[k,:] = T[piv[k], 3S:4S), G_j from T[:, S:2S),
-// H_j from T[:, 2S:3S)  (column-major S x S outputs).
+// H_j from T[:, 2S:3S)  (column-major S x S outputs), all shifts.
 template <typename C>
-__global__ void k_extract(const C *__restrict__ Tall, int S, const int *__restrict__ pivall, C *__restrict__ Dinv,
-                          C *__restrict__ G, C *__restrict__ H, BcrLevel lv, int nodd, int top) {
-    const int64_t SS = (int64_t)S * S, total = (int64_t)nodd * SS;
+__global__ void k_extract(FV<C> v, BcrLevel lv, int nodd, int top, int nshift) {
+    const int S = v.S;
+    const int64_t SS = (int64_t)S * S, pershift = (int64_t)nodd * SS, total = pershift * nshift;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
          idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t o = idx / SS;
-        const int64_t w = idx - o * SS;
+        const int64_t sh = idx / pershift;
+        const int64_t ws = idx - sh * pershift;
+        const int64_t o = ws / SS;
+        const int64_t w = ws - o * SS;
         const int c = (int)(w / S), k = (int)(w - (int64_t)c * S);
-        const C *T = Tall + o * 4 * SS;
-        const int p = pivall[o * S + k];
+        const C *T = v.T + sh * v.t_stride + o * 4 * SS;
+        const int p = v.piv[sh * v.p_stride + o * S + k];
         const int64_t j = top ? 0 : (2 * o + 1) * lv.stride;
-        Dinv[j * SS + w] = T[p + (int64_t)(3 * S + c) * S];
+        const int64_t out = sh * v.f_stride + j * SS + w;
+        v.Dinv[out] = T[p + (int64_t)(3 * S + c) * S];
         if (!top) {
-            G[j * SS + w] = T[p + (int64_t)(S + c) * S];
-            H[j * SS + w] = T[p + (int64_t)(2 * S + c) * S];
+            v.G[out] = T[p + (int64_t)(S + c) * S];
+            v.H[out] = T[p + (int64_t)(2 * S + c) * S];
         }
     }
 }
 
 // Level 0 update of the even blocks with the sparse couplings of the CSR:
 //   Dw_i -= rs (L_i H_jl + U_i G_jr),  L'_i = -rs L_i G_jl,  U'_i = -rs U_i H_jr.
-// CTA = (chunk of CW columns, even index e); one thread per row.
+// CTA = (chunk of CW columns, even index e, shift); one thread per row.
 constexpr int kEvenCW = 8;
 template <typename C>
-__global__ void k_even_l0(C *__restrict__ Dw, C *__restrict__ LU, const C *__restrict__ G, const C *__restrict__ H,
-                          int S, BcrLevel lv, const int *__restrict__ arow, const int *__restrict__ acol,
-                          const double2 *__restrict__ aval, const int *__restrict__ asplit,
-                          const double *__restrict__ rscale) {
+__global__ void k_even_l0(FV<C> v, BcrLevel lv) {
+    const int S = v.S;
     const int64_t SS = (int64_t)S * S;
-    const int64_t e = blockIdx.y;
+    const int64_t e = blockIdx.y, sh = blockIdx.z;
     const int64_t q = 2 * e;                 // position = original block at level 0
     const bool hasl = q >= 1, hasr = q + 1 < lv.Kl;
     const bool outl = (lv.lu_nL >= 0) && q >= 2, outr = (lv.lu_nU >= 0) && q + 2 < lv.Kl;
     const int c0 = blockIdx.x * kEvenCW;
     const int cn = min(kEvenCW, S - c0);
-    C *Di = Dw + q * SS;
+    C *Di = v.Dw + sh * v.f_stride + q * SS;
+    const C *G = v.G + sh * v.f_stride, *H = v.H + sh * v.f_stride;
+    C *LU = v.LU + sh * v.lu_stride;
+    const double *rscale = v.rscale + sh * v.np;
     for (int r = threadIdx.x; r < S; r += blockDim.x) {
         const int64_t p = q * S + r;
-        const int l0 = arow[p], l1 = asplit[2 * p], u0 = asplit[2 * p + 1], u1 = arow[p + 1];
+        const int l0 = v.arow[p], l1 = v.asplit[2 * p], u0 = v.asplit[2 * p + 1], u1 = v.arow[p + 1];
         const double rs = rscale[p];
         for (int t = 0; t < cn; ++t) {
             const int64_t col = (int64_t)(c0 + t) * S;
             C dsum = czero<C>(), lsum = czero<C>(), usum = czero<C>();
             if (hasl)
                 for (int k = l0; k < l1; ++k) {
-                    const C a = from_c128<C>(rs * aval[k]);
-                    const int64_t cr = acol[k] - (q - 1) * S;
+                    const C a = from_c128<C>(rs * v.aval[k]);
+                    const int64_t cr = v.acol[k] - (q - 1) * S;
                     dsum = cfma(dsum, a, H[(q - 1) * SS + cr + col]);
                     if (outl) lsum = cfma(lsum, a, G[(q - 1) * SS + cr + col]);
                 }
             if (hasr)
                 for (int k = u0; k < u1; ++k) {
-                    const C a = from_c128<C>(rs * aval[k]);
-                    const int64_t cr = acol[k] - (q + 1) * S;
+                    const C a = from_c128<C>(rs * v.aval[k]);
+                    const int64_t cr = v.acol[k] - (q + 1) * S;
                     dsum = cfma(dsum, a, G[(q + 1) * SS + cr + col]);
                     if (outr) usum = cfma(usum, a, H[(q + 1) * SS + cr + col]);
                 }
@@ -355,27 +397,32 @@ __global__ void k_even_l0(C *__restrict__ Dw, C *__restrict__ LU, const C *__res
 }
 
 // Batched dense update of the even blocks at levels >= 1, one GEMM job per
-// (even block, kind): kind 0: Dw_i -= L_q H_jl + U_q G_jr;  kind 1: L' = -L_q G_jl;
+// (shift, even block, kind): kind 0: Dw_i -= L_q H_jl + U_q G_jr;  kind 1: L' = -L_q G_jl;
 // kind 2: U' = -U_q H_jr.  Column-major S x S complex, 64 x 64 tiles, 4 x 4 per thread.
 constexpr int kGT = 64, kGK = 16;
 template <typename C>
-__global__ void __launch_bounds__(256) k_even_gemm(C *__restrict__ Dw, C *__restrict__ LU, const C *__restrict__ G,
-                                                   const C *__restrict__ H, int S, BcrLevel lv) {
+__global__ void __launch_bounds__(256) k_even_gemm(FV<C> v, BcrLevel lv, int job0) {
     __shared__ C As[kGK][kGT + 1];
     __shared__ C Bs[kGK][kGT + 1];
+    const int S = v.S;
     const int64_t SS = (int64_t)S * S;
-    const int job = blockIdx.z;
-    const int64_t e = job / 3;
-    const int kind = job - 3 * (int)e;
+    const int job = job0 + blockIdx.z;
+    const int per = 3 * lv.neven;
+    const int64_t sh = job / per;
+    const int jj = job - (int)sh * per;
+    const int64_t e = jj / 3;
+    const int kind = jj - 3 * (int)e;
     const int64_t q = 2 * e;
     const bool hasl = q >= 1, hasr = q + 1 < lv.Kl;
     const C *A1 = nullptr, *B1 = nullptr, *A2 = nullptr, *B2 = nullptr;
     C *Cm = nullptr;
     bool accumulate = false;
+    C *LU = v.LU + sh * v.lu_stride;
+    const C *G = v.G + sh * v.f_stride, *H = v.H + sh * v.f_stride;
     const C *Lq = LU + (lv.lu_L + q) * SS, *Uq = LU + (lv.lu_U + q) * SS;
     const int64_t jl = (q - 1) * lv.stride, jr = (q + 1) * lv.stride;
     if (kind == 0) {
-        Cm = Dw + q * lv.stride * SS;
+        Cm = v.Dw + sh * v.f_stride + q * lv.stride * SS;
         accumulate = true;
         if (hasl) { A1 = Lq; B1 = H + jl * SS; }
         if (hasr) { A2 = Uq; B2 = G + jr * SS; }
@@ -442,39 +489,37 @@ unsigned grid_for(int64_t work, int threads, int num_sms) {
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + threads - 1) / threads, 16LL * num_sms));
 }
 
-// Gauss-Jordan of the nodd work matrices T_o (all panels), then extraction.
+// Gauss-Jordan of the nodd work matrices T_o of every shift (all panels), then extraction.
 template <typename C, int NB>
-int gauss_jordan(kore_plan *p, const BcrLevel &lv, int nodd, int top) {
+int gauss_jordan(kore_plan *p, const FV<C> &v, const BcrLevel &lv, int nodd, int top, int nshift) {
     const int S = p->S;
-    C *T = static_cast<C *>(p->d_T);
     const size_t smem = (size_t)S * NB * sizeof(C) + (size_t)S * sizeof(int);
     KORE_CUDA_TRY(cudaFuncSetAttribute(k_panel<C, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int pthreads = std::min(1024, ((S + 31) / 32) * 32);
     for (int k0 = 0; k0 < S; k0 += NB) {
         const int nb = std::min(NB, S - k0);
-        k_panel<C, NB><<<nodd, pthreads, smem, p->stream>>>(T, S, k0, p->d_piv, p->d_pidx, p->d_used, p->d_err);
+        k_panel<C, NB><<<dim3(nodd, nshift), pthreads, smem, p->stream>>>(v, k0);
         KORE_LAUNCHED(1);
         const int cb = k0 + nb;
         if (!top) {
             // trailing columns: the rest of D, the L, U and identity columns
-            dim3 g(kore_div_up(4 * S - cb, kUpdTW), nodd);
-            k_update<C, NB, kUpdTW><<<g, 256, 0, p->stream>>>(T, S, k0, nb, cb, 4 * S, p->d_piv, p->d_pidx);
+            dim3 g(kore_div_up(4 * S - cb, kUpdTW), nodd, nshift);
+            k_update<C, NB, kUpdTW><<<g, 256, 0, p->stream>>>(v, k0, nb, cb, 4 * S);
             KORE_LAUNCHED(1);
         } else {
             // the top block has no L, U columns: the rest of D, then the identity columns
             if (cb < S) {
-                dim3 g(kore_div_up(S - cb, kUpdTW), nodd);
-                k_update<C, NB, kUpdTW><<<g, 256, 0, p->stream>>>(T, S, k0, nb, cb, S, p->d_piv, p->d_pidx);
+                dim3 g(kore_div_up(S - cb, kUpdTW), nodd, nshift);
+                k_update<C, NB, kUpdTW><<<g, 256, 0, p->stream>>>(v, k0, nb, cb, S);
                 KORE_LAUNCHED(1);
             }
-            dim3 g(kore_div_up(S, kUpdTW), nodd);
-            k_update<C, NB, kUpdTW><<<g, 256, 0, p->stream>>>(T, S, k0, nb, 3 * S, 4 * S, p->d_piv, p->d_pidx);
+            dim3 g(kore_div_up(S, kUpdTW), nodd, nshift);
+            k_update<C, NB, kUpdTW><<<g, 256, 0, p->stream>>>(v, k0, nb, 3 * S, 4 * S);
             KORE_LAUNCHED(1);
         }
     }
-    k_extract<C><<<grid_for((int64_t)nodd * S * S, 256, p->num_sms), 256, 0, p->stream>>>(
-        T, S, p->d_piv, static_cast<C *>(p->d_Dinv), static_cast<C *>(p->d_Gm), static_cast<C *>(p->d_Hm), lv,
-        nodd, top);
+    k_extract<C><<<grid_for((int64_t)nodd * S * S * nshift, 256, p->num_sms), 256, 0, p->stream>>>(v, lv, nodd, top,
+                                                                                                nshift);
     KORE_LAUNCHED(1);
     KORE_CUDA_TRY(cudaGetLastError());
     return KORE_OK;
@@ -482,37 +527,37 @@ int gauss_jordan(kore_plan *p, const BcrLevel &lv, int nodd, int top) {
 
 template <typename C, int NB>
 int factor_levels(kore_plan *p) {
-    const int S = p->S, K = p->K;
+    const int S = p->S, K = p->K, ns = p->nshift;
     const int64_t SS = (int64_t)S * S;
     cudaStream_t st = p->stream;
-    C *Dw = static_cast<C *>(p->d_Dw), *LU = static_cast<C *>(p->d_LU), *T = static_cast<C *>(p->d_T);
-    C *G = static_cast<C *>(p->d_Gm), *H = static_cast<C *>(p->d_Hm);
+    const FV<C> v = make_fv<C>(p);
     // working diagonal blocks from the CSR
-    k_Dw_init<C><<<grid_for((int64_t)K * SS, 256, p->num_sms), 256, 0, st>>>(Dw, K, S, p->d_bsz);
-    k_Dw_scatter<C><<<grid_for(p->np * 32, 256, p->num_sms), 256, 0, st>>>(
-        Dw, p->np, S, p->d_arow, p->d_acol, p->d_aval, p->d_asplit, p->d_brow, p->d_bcol, p->d_bval,
-        p->has_b ? 1 : 0, p->sigma_re, p->sigma_im, p->d_rscale);
+    k_Dw_init<C><<<grid_for((int64_t)K * SS * ns, 256, p->num_sms), 256, 0, st>>>(v, ns);
+    k_Dw_scatter<C><<<grid_for(p->np * 32 * ns, 256, p->num_sms), 256, 0, st>>>(v, ns);
     KORE_LAUNCHED(2);
     for (int l = 0; l < p->nlev; ++l) {
         const BcrLevel &lv = p->lev[l];
-        k_T_fill<C><<<grid_for((int64_t)lv.nodd * 4 * SS, 256, p->num_sms), 256, 0, st>>>(T, Dw, LU, S, lv, lv.nodd);
+        k_T_fill<C><<<grid_for((int64_t)lv.nodd * 4 * SS * ns, 256, p->num_sms), 256, 0, st>>>(v, lv, lv.nodd, ns);
         KORE_LAUNCHED(1);
         if (l == 0) {
-            k_T_scatter_LU<C><<<grid_for((int64_t)lv.nodd * S * 32, 256, p->num_sms), 256, 0, st>>>(
-                T, S, lv.nodd, p->d_arow, p->d_acol, p->d_aval, p->d_asplit, p->d_rscale);
+            k_T_scatter_LU<C><<<grid_for((int64_t)lv.nodd * S * 32 * ns, 256, p->num_sms), 256, 0, st>>>(v, lv.nodd,
+                                                                                                        ns);
             KORE_LAUNCHED(1);
         }
-        KORE_TRY((gauss_jordan<C, NB>(p, lv, lv.nodd, 0)));
+        KORE_TRY((gauss_jordan<C, NB>(p, v, lv, lv.nodd, 0, ns)));
         if (l == 0) {
-            dim3 g(kore_div_up(S, kEvenCW), lv.neven);
+            dim3 g(kore_div_up(S, kEvenCW), lv.neven, ns);
             const int th = std::min(1024, ((S + 31) / 32) * 32);
-            k_even_l0<C><<<g, th, 0, st>>>(Dw, LU, G, H, S, lv, p->d_arow, p->d_acol, p->d_aval, p->d_asplit,
-                                          p->d_rscale);
+            k_even_l0<C><<<g, th, 0, st>>>(v, lv);
+            KORE_LAUNCHED(1);
         } else {
-            dim3 g(kore_div_up(S, kGT), kore_div_up(S, kGT), 3 * lv.neven);
-            k_even_gemm<C><<<g, 256, 0, st>>>(Dw, LU, G, H, S, lv);
+            const int jobs = 3 * lv.neven * ns;
+            for (int j0 = 0; j0 < jobs; j0 += 65535) {
+                dim3 g(kore_div_up(S, kGT), kore_div_up(S, kGT), std::min(65535, jobs - j0));
+                k_even_gemm<C><<<g, 256, 0, st>>>(v, lv, j0);
+                KORE_LAUNCHED(1);
+            }
         }
-        KORE_LAUNCHED(1);
         KORE_CUDA_TRY(cudaGetLastError());
     }
     // the last active block (block 0): T = [Dw_0 | 0 | 0 | I]; stride 0 maps odd index 0 to block 0
@@ -520,9 +565,9 @@ int factor_levels(kore_plan *p) {
     top.Kl = 1;
     top.stride = 0;
     top.lu_L = top.lu_U = top.lu_nL = top.lu_nU = -1;
-    k_T_fill<C><<<grid_for(4 * SS, 256, p->num_sms), 256, 0, st>>>(T, Dw, LU, S, top, 1);
+    k_T_fill<C><<<grid_for(4 * SS * ns, 256, p->num_sms), 256, 0, st>>>(v, top, 1, ns);
     KORE_LAUNCHED(1);
-    KORE_TRY((gauss_jordan<C, NB>(p, top, 1, 1)));
+    KORE_TRY((gauss_jordan<C, NB>(p, v, top, 1, 1, ns)));
     return KORE_OK;
 }
 
@@ -572,46 +617,103 @@ void kore_build_levels(kore_plan *p) {
     p->lu_mats = std::max<int64_t>(lu, 1);
 }
 
-int kore_factor_impl(kore_plan *p, double sre, double sim, int precision) {
-    if (precision != KORE_PREC_FP64 && precision != KORE_PREC_MIXED) return KORE_EINVAL;
-    const size_t elt = (precision == KORE_PREC_FP64) ? sizeof(double2) : sizeof(float2);
-    const int64_t SS = (int64_t)p->S * p->S;
-    if (p->factor_elt != elt) {
-        void **bufs[] = {&p->d_Dinv, &p->d_Gm, &p->d_Hm, &p->d_Dw, &p->d_LU, &p->d_T, &p->d_zlo, &p->d_xlo, &p->d_flo};
-        for (void **b : bufs) {
-            if (*b) cudaFree(*b);
-            *b = nullptr;
-        }
-        p->factor_elt = 0;
-        KORE_TRY(kore_alloc(p, &p->d_Dinv, (size_t)p->K * SS * elt));
-        KORE_TRY(kore_alloc(p, &p->d_Gm, (size_t)p->K * SS * elt));
-        KORE_TRY(kore_alloc(p, &p->d_Hm, (size_t)p->K * SS * elt));
-        KORE_TRY(kore_alloc(p, &p->d_Dw, (size_t)p->K * SS * elt));
-        KORE_TRY(kore_alloc(p, &p->d_LU, (size_t)p->lu_mats * SS * elt));
-        KORE_TRY(kore_alloc(p, &p->d_T, (size_t)p->nodd_max * 4 * SS * elt));
-        KORE_TRY(kore_alloc(p, &p->d_zlo, (size_t)p->np * elt));
-        KORE_TRY(kore_alloc(p, &p->d_xlo, (size_t)p->np * elt));
-        KORE_TRY(kore_alloc(p, &p->d_flo, (size_t)p->np * elt));
-        KORE_CUDA_TRY(cudaMemset(p->d_LU, 0, (size_t)p->lu_mats * SS * elt));
-        p->factor_elt = elt;
+namespace {
+
+// (Re)allocate the per-shift buffers for `cap` shifts of elements of `elt` bytes.
+int ensure_factor_storage(kore_plan *p, int cap, size_t elt) {
+    if (p->factor_elt == elt && p->shift_cap >= cap) return KORE_OK;
+    void **bufs[] = {&p->d_Dinv, &p->d_Gm, &p->d_Hm, &p->d_Dw, &p->d_LU, &p->d_T, &p->d_zlo, &p->d_xlo, &p->d_flo,
+                     (void **)&p->d_rscale, (void **)&p->d_piv, (void **)&p->d_pidx, (void **)&p->d_used,
+                     (void **)&p->d_sigma, (void **)&p->d_minf, (void **)&p->d_bb, (void **)&p->d_xb, (void **)&p->d_rb,
+                     (void **)&p->d_bn, (void **)&p->d_rn, (void **)&p->d_part, (void **)&p->d_ir,
+                     (void **)&p->d_cnt};
+    for (void **b : bufs) {
+        if (*b) cudaFree(*b);
+        *b = nullptr;
     }
+    p->bytes -= p->factor_bytes;
+    p->factor_bytes = 0;
+    p->factor_elt = 0;
+    p->shift_cap = 0;
+    const size_t before = p->bytes;
+    const size_t c = (size_t)cap;
+    KORE_TRY(kore_alloc(p, &p->d_Dinv, c * p->f_stride() * elt));
+    KORE_TRY(kore_alloc(p, &p->d_Gm, c * p->f_stride() * elt));
+    KORE_TRY(kore_alloc(p, &p->d_Hm, c * p->f_stride() * elt));
+    KORE_TRY(kore_alloc(p, &p->d_Dw, c * p->f_stride() * elt));
+    KORE_TRY(kore_alloc(p, &p->d_LU, c * p->lu_stride() * elt));
+    KORE_TRY(kore_alloc(p, &p->d_T, c * p->t_stride() * elt));
+    KORE_TRY(kore_alloc(p, &p->d_zlo, c * p->np * elt));
+    KORE_TRY(kore_alloc(p, &p->d_xlo, c * p->np * elt));
+    KORE_TRY(kore_alloc(p, &p->d_flo, c * p->np * elt));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_rscale, c * p->np * sizeof(double)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_piv, c * p->p_stride() * sizeof(int)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_pidx, c * p->p_stride() * sizeof(int)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_used, c * p->p_stride() * sizeof(int)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_sigma, c * sizeof(double2)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_minf, c * sizeof(double)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_bb, c * p->np * sizeof(double2)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_xb, c * p->np * sizeof(double2)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_rb, c * p->np * sizeof(double2)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_bn, c * sizeof(double)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_rn, c * sizeof(double)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_part, c * 2 * (size_t)kore_div_up(p->np * 16, 256) * sizeof(double)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_ir, c * sizeof(IrState)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_cnt, c * (size_t)(3 * p->nlev + 1) * p->K * sizeof(int)));
+    KORE_CUDA_TRY(cudaMemset(p->d_LU, 0, c * p->lu_stride() * elt));
+    KORE_CUDA_TRY(cudaMemset(p->d_piv, 0, c * p->p_stride() * sizeof(int)));
+    KORE_CUDA_TRY(cudaMemset(p->d_pidx, 0xff, c * p->p_stride() * sizeof(int)));
+    KORE_CUDA_TRY(cudaMemset(p->d_used, 0, c * p->p_stride() * sizeof(int)));
+    KORE_CUDA_TRY(cudaMemset(p->d_ir, 0, c * sizeof(IrState)));
+    p->factor_bytes = p->bytes - before;
+    p->factor_elt = elt;
+    p->shift_cap = cap;
+    return KORE_OK;
+}
+
+}  // namespace
+
+int kore_factor_impl(kore_plan *p, int nshift, const double *sigmas, int precision) {
+    if (precision != KORE_PREC_FP64 && precision != KORE_PREC_MIXED) return KORE_EINVAL;
+    if (nshift <= 0 || !sigmas) return KORE_EINVAL;
+    const size_t elt = (precision == KORE_PREC_FP64) ? sizeof(double2) : sizeof(float2);
     p->factored = false;
+    KORE_TRY(ensure_factor_storage(p, nshift, elt));
     p->prec = precision;
-    p->sigma_re = sre;
-    p->sigma_im = sim;
-    const unsigned grid = std::min<unsigned>(kore_div_up(p->np, 256), 1024u);
-    k_rowinfo<<<grid, 256, 0, p->stream>>>(p->np, p->d_arow, p->d_aval, p->d_brow, p->d_bval,
-                                           p->has_b ? 1 : 0, std::hypot(sre, sim), p->d_rscale, p->d_red);
-    KORE_LAUNCHED(1);
-    KORE_CUDA_TRY(cudaMemcpyAsync(p->h_red, p->d_red, grid * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+    p->nshift = nshift;
+    p->sigmas.assign(nshift, mk(0.0, 0.0));
+    for (int s = 0; s < nshift; ++s) p->sigmas[s] = mk(sigmas[2 * s], sigmas[2 * s + 1]);
+    p->sigma_re = sigmas[0];
+    p->sigma_im = sigmas[1];
+    KORE_CUDA_TRY(cudaMemcpyAsync(p->d_sigma, p->sigmas.data(), nshift * sizeof(double2), cudaMemcpyHostToDevice,
+                                  p->stream));
+    const unsigned grid = std::min<unsigned>(kore_div_up(p->np, 256), 64u);
+    std::vector<double> red((size_t)grid * nshift);
+    double *d_red = p->d_part;   // scratch: grid x nshift doubles fit the residual partials buffer
     if (p->prof) KORE_TRY(kore_prof_mark(p, 1, true));
-    int s = (precision == KORE_PREC_FP64) ? factor_dispatch<double2>(p) : factor_dispatch<float2>(p);
+    int s;
+    if (precision == KORE_PREC_FP64) {
+        k_rowinfo<double2><<<dim3(grid, nshift), 256, 0, p->stream>>>(make_fv<double2>(p), d_red);
+        KORE_LAUNCHED(1);
+        KORE_CUDA_TRY(cudaMemcpyAsync(red.data(), d_red, red.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+        KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+        s = factor_dispatch<double2>(p);
+    } else {
+        k_rowinfo<float2><<<dim3(grid, nshift), 256, 0, p->stream>>>(make_fv<float2>(p), d_red);
+        KORE_LAUNCHED(1);
+        KORE_CUDA_TRY(cudaMemcpyAsync(red.data(), d_red, red.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+        KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+        s = factor_dispatch<float2>(p);
+    }
     if (s != KORE_OK) return s;
     if (p->prof) KORE_TRY(kore_prof_mark(p, 1, false));
+    p->minfs.assign(nshift, 0.0);
+    for (int sh = 0; sh < nshift; ++sh)
+        for (unsigned b = 0; b < grid; ++b) p->minfs[sh] = std::max(p->minfs[sh], red[(size_t)sh * grid + b]);
+    p->minf = p->minfs[0];
+    KORE_CUDA_TRY(cudaMemcpyAsync(p->d_minf, p->minfs.data(), nshift * sizeof(double), cudaMemcpyHostToDevice,
+                                  p->stream));
     KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
-    double mx = 0.0;
-    for (unsigned b = 0; b < grid; ++b) mx = std::max(mx, p->h_red[b]);
-    p->minf = mx;
     KORE_TRY(kore_check_device_error(p));
     p->factored = true;
     return KORE_OK;

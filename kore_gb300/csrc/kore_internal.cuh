@@ -60,32 +60,48 @@ struct kore_plan {
     // blocks i = q * 2^l; the odd positions are eliminated, the even ones carry on.
     int prec = -1;
     bool factored = false;
-    double sigma_re = 0, sigma_im = 0;
-    double minf = 0;                  // ||A - sigma B||_inf
+    // factorised shifts: every factor buffer holds shift_cap sets, shift s at offset s * stride
+    int nshift = 0, shift_cap = 0;
+    std::vector<double2> sigmas;      // host copy of the shifts
+    std::vector<double> minfs;        // ||A - sigma_s B||_inf per shift
+    double2 *d_sigma = nullptr;       // device copy of the shifts
+    double *d_minf = nullptr;
+    double sigma_re = 0, sigma_im = 0;   // shift 0 (the eigensolver's target)
+    double minf = 0;                     // ||A - sigma_0 B||_inf
     size_t factor_elt = 0;            // bytes of one complex element of the factors
     int nlev = 0;                     // reduction levels (the top block is solved after them)
     std::vector<struct BcrLevel> lev; // host copy of the level table
     struct BcrLevel *d_lev = nullptr; // device copy
     int64_t lu_mats = 0;              // dense coupling matrices of levels >= 1
     int nodd_max = 1;                 // largest number of blocks eliminated at one level
-    // S x S column-major blocks, indexed by original block number
+    // S x S column-major blocks, indexed by original block number, per shift
     void *d_Dinv = nullptr, *d_Gm = nullptr, *d_Hm = nullptr, *d_Dw = nullptr;
-    void *d_LU = nullptr;             // lu_mats blocks
-    void *d_T = nullptr;              // nodd_max x (S x 4S) Gauss-Jordan work, column-major
-    double *d_rscale = nullptr;       // np row equilibration factors
-    int *d_piv = nullptr;             // nodd_max x S: pivot row chosen for column k
-    int *d_pidx = nullptr;            // nodd_max x S: position of a row in the current panel or -1
-    int *d_used = nullptr;            // nodd_max x S: row already used as a pivot
+    void *d_LU = nullptr;             // lu_mats blocks per shift
+    void *d_T = nullptr;              // nodd_max x (S x 4S) Gauss-Jordan work per shift, column-major
+    double *d_rscale = nullptr;       // np row equilibration factors per shift
+    int *d_piv = nullptr;             // nodd_max x S per shift: pivot row chosen for column k
+    int *d_pidx = nullptr;            // nodd_max x S per shift: position of a row in the current panel or -1
+    int *d_used = nullptr;            // nodd_max x S per shift: row already used as a pivot
+
+    int64_t f_stride() const { return (int64_t)K * S * S; }
+    int64_t lu_stride() const { return lu_mats * (int64_t)S * S; }
+    int64_t t_stride() const { return (int64_t)nodd_max * 4 * S * S; }
+    int64_t p_stride() const { return (int64_t)nodd_max * S; }
 
     // solve workspace (padded, complex128 unless noted)
     double2 *d_v[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    void *d_zlo = nullptr, *d_xlo = nullptr, *d_flo = nullptr;   // sweep vectors in factor precision
+    // per shift (shift_cap sets of np): sweep vectors in factor precision, and the
+    // complex128 right-hand side, solution and residual of a batched solve
+    void *d_zlo = nullptr, *d_xlo = nullptr, *d_flo = nullptr;
+    double2 *d_bb = nullptr, *d_xb = nullptr, *d_rb = nullptr;
+    double *d_bn = nullptr, *d_rn = nullptr;   // per-shift ||b||_inf and ||r||_inf
     double *d_red = nullptr;          // reduction scratch (8192 doubles)
-    double *d_part = nullptr;         // per-CTA maxima of the residual kernel (2 per CTA)
+    double *d_part = nullptr;         // per-CTA maxima of the residual kernel (2 per CTA, per shift)
     double *h_red = nullptr;          // pinned host mirror
     int *d_err = nullptr;
     unsigned *d_bar = nullptr;
-    IrState *d_ir = nullptr;
+    int *d_cnt = nullptr;             // sweep completion counters (shift_cap x (3 nlev + 1) x K)
+    IrState *d_ir = nullptr;          // one per shift
 
     // Krylov-Schur workspace
     double2 *d_V = nullptr;           // np x (ncv+1)
@@ -94,6 +110,7 @@ struct kore_plan {
     double2 *d_small = nullptr;
 
     size_t bytes = 0;
+    size_t factor_bytes = 0;          // bytes of the per-shift buffers
     int sweep_occ[2] = {0, 0};        // co-resident sweep CTAs per SM (complex64, complex128)
     int last_refine_iters = 0;
     double last_resid = 0;
@@ -120,11 +137,13 @@ int kore_alloc(kore_plan *p, void **ptr, size_t bytes);
 
 // factor.cu
 void kore_build_levels(kore_plan *p);
-int kore_factor_impl(kore_plan *p, double sre, double sim, int precision);
+// factorise A - sigma_s B for nshift shifts (interleaved re, im) at once
+int kore_factor_impl(kore_plan *p, int nshift, const double *sigmas, int precision);
 
 // sweep.cu
-// x = (A - sigma B)^-1 b on padded l-major complex128 vectors (device), refined in
-// FP64 when the factors are complex64 (asynchronous; counters in the plan's IrState).
+// x_s = (A - sigma_s B)^-1 b_s for every factorised shift s on padded l-major
+// complex128 vectors (device; shift s at offset s * np), refined in FP64 when the
+// factors are complex64 (asynchronous; counters in the plan's per-shift IrState).
 int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol);
 int kore_ir_reset(kore_plan *p);
 int kore_ir_read(kore_plan *p, IrState *out);
@@ -134,6 +153,9 @@ int kore_spmv_b(kore_plan *p, const double2 *x, double2 *y);
 int kore_spmv_pencil(kore_plan *p, double lre, double lim, const double2 *x, double2 *y);
 int kore_gather(kore_plan *p, const double2 *orig, double2 *padded);
 int kore_scatter(kore_plan *p, const double2 *padded, double2 *orig);
+// nshift vectors at once (original order: shift s at s * n; padded: at s * np)
+int kore_gather_shifts(kore_plan *p, const double2 *orig, double2 *padded);
+int kore_scatter_shifts(kore_plan *p, const double2 *padded, double2 *orig);
 
 // eigs.cu
 int kore_eigs_impl(kore_plan *p, const kore_eps_opts *o, double *evals, double *evecs,

@@ -95,7 +95,8 @@ void free_plan(kore_plan *p) {
     void *ptrs[] = {p->d_arow, p->d_acol, p->d_asplit, p->d_aval, p->d_brow, p->d_bcol, p->d_bval,
                     p->d_slot2orig, p->d_bsz, p->d_Dinv, p->d_Gm, p->d_Hm, p->d_Dw, p->d_LU, p->d_lev,
                     p->d_rscale, p->d_T, p->d_piv, p->d_pidx, p->d_used, p->d_zlo, p->d_xlo, p->d_flo,
-                    p->d_red, p->d_part, p->d_err, p->d_bar, p->d_ir, p->d_V, p->d_Vtmp, p->d_small};
+                    p->d_red, p->d_part, p->d_err, p->d_bar, p->d_ir, p->d_V, p->d_Vtmp, p->d_small,
+                    p->d_sigma, p->d_minf, p->d_bb, p->d_xb, p->d_rb, p->d_bn, p->d_rn, p->d_cnt};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     for (auto &v : p->d_v)
@@ -212,27 +213,16 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
     }
     KORE_TRY(upload(p, &p->d_slot2orig, slot2orig));
     KORE_TRY(upload(p, &p->d_bsz, p->bsz));
-    KORE_TRY(kore_alloc(p, (void **)&p->d_rscale, p->np * sizeof(double)));
     kore_build_levels(p);
     if (!p->lev.empty()) {
         KORE_TRY(kore_alloc(p, (void **)&p->d_lev, p->lev.size() * sizeof(BcrLevel)));
         KORE_CUDA_TRY(cudaMemcpy(p->d_lev, p->lev.data(), p->lev.size() * sizeof(BcrLevel), cudaMemcpyHostToDevice));
     }
-    KORE_TRY(kore_alloc(p, (void **)&p->d_piv, (size_t)p->nodd_max * p->S * sizeof(int)));
-    KORE_TRY(kore_alloc(p, (void **)&p->d_pidx, (size_t)p->nodd_max * p->S * sizeof(int)));
-    KORE_TRY(kore_alloc(p, (void **)&p->d_used, (size_t)p->nodd_max * p->S * sizeof(int)));
     for (auto &v : p->d_v) KORE_TRY(kore_alloc(p, (void **)&v, p->np * sizeof(double2)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_red, 8192 * sizeof(double)));
-    // one pair of maxima per CTA of the residual kernel (16 lanes per row, 256 threads)
-    KORE_TRY(kore_alloc(p, (void **)&p->d_part, 2 * (size_t)kore_div_up(p->np * 16, 256) * sizeof(double)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_err, sizeof(int)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_bar, 64));
-    KORE_TRY(kore_alloc(p, (void **)&p->d_ir, sizeof(IrState)));
-    KORE_CUDA_TRY(cudaMemset(p->d_ir, 0, sizeof(IrState)));
     KORE_CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
-    KORE_CUDA_TRY(cudaMemset(p->d_piv, 0, (size_t)p->nodd_max * p->S * sizeof(int)));
-    KORE_CUDA_TRY(cudaMemset(p->d_pidx, 0xff, (size_t)p->nodd_max * p->S * sizeof(int)));
-    KORE_CUDA_TRY(cudaMemset(p->d_used, 0, (size_t)p->nodd_max * p->S * sizeof(int)));
     KORE_CUDA_TRY(cudaMemset(p->d_red, 0, 8192 * sizeof(double)));
     KORE_CUDA_TRY(cudaMallocHost(&p->h_red, 8192 * sizeof(double)));
     KORE_CUDA_TRY(cudaDeviceSynchronize());
@@ -240,21 +230,24 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
     return KORE_OK;
 }
 
+// nrhs right-hand sides (original order, device) in groups of nshift: right-hand side k
+// is solved with shift k % nshift.
 int solve_dev_impl(kore_plan *p, const double2 *b, double2 *x, int nrhs, double tol, kore_stats *st) {
+    if (nrhs % p->nshift != 0) return KORE_EINVAL;
     KORE_TRY(kore_ir_reset(p));
-    for (int k = 0; k < nrhs; ++k) {
-        KORE_TRY(kore_gather(p, b + (int64_t)k * p->n, p->d_v[0]));
-        KORE_TRY(kore_apply_inverse(p, p->d_v[0], p->d_v[1], tol));
-        KORE_TRY(kore_scatter(p, p->d_v[1], x + (int64_t)k * p->n));
+    for (int g = 0; g < nrhs; g += p->nshift) {
+        KORE_TRY(kore_gather_shifts(p, b + (int64_t)g * p->n, p->d_bb));
+        KORE_TRY(kore_apply_inverse(p, p->d_bb, p->d_xb, tol));
+        KORE_TRY(kore_scatter_shifts(p, p->d_xb, x + (int64_t)g * p->n));
     }
+    IrState s;
+    KORE_TRY(kore_ir_read(p, &s));
     if (st) {
-        IrState s;
-        KORE_TRY(kore_ir_read(p, &s));
         st->sweeps = s.sweeps;
         st->refine_iters_max = s.iters_max;
         st->solve_resid_max = s.eta_max;
-        if (s.nan) return KORE_ENAN;
     }
+    if (s.nan) return KORE_ENAN;
     return KORE_OK;
 }
 
@@ -270,11 +263,19 @@ int kore_plan_create(const kore_pencil_desc *desc, int device, kore_plan **plan)
 int kore_factor(kore_plan *plan, double sigma_re, double sigma_im, int precision) {
     if (!plan) return KORE_EINVAL;
     DeviceGuard g(plan->device);
-    return kore_factor_impl(plan, sigma_re, sigma_im, precision);
+    const double sig[2] = {sigma_re, sigma_im};
+    return kore_factor_impl(plan, 1, sig, precision);
+}
+
+int kore_factor_shifts(kore_plan *plan, int nshift, const double *sigmas, int precision) {
+    if (!plan || nshift <= 0 || !sigmas) return KORE_EINVAL;
+    DeviceGuard g(plan->device);
+    return kore_factor_impl(plan, nshift, sigmas, precision);
 }
 
 int kore_solve(kore_plan *p, const double *b, double *x, int nrhs, double refine_tol, kore_stats *stats) {
     if (!p || !b || !x || nrhs <= 0) return KORE_EINVAL;
+    if (p->factored && nrhs % p->nshift != 0) return KORE_EINVAL;
     if (!p->factored) return KORE_ENOTFACTORED;
     DeviceGuard g(p->device);
     auto t0 = std::chrono::steady_clock::now();
@@ -320,6 +321,7 @@ int kore_solve_dev(kore_plan *p, const void *b_dev, void *x_dev, int nrhs, doubl
 int kore_eigs(kore_plan *p, const kore_eps_opts *opts, double *evals, double *evecs, int max_pairs, int *nconv,
               kore_stats *stats) {
     if (!p || !opts || !evals || !nconv || max_pairs <= 0) return KORE_EINVAL;
+    if (p->factored && p->nshift != 1) return KORE_EINVAL;
     DeviceGuard g(p->device);
     *nconv = 0;
     return kore_eigs_impl(p, opts, evals, evecs, max_pairs, nconv, stats);
@@ -348,8 +350,8 @@ int kore_profile(kore_plan *p, int enable, double *out) {
     if (!p) return KORE_EINVAL;
     DeviceGuard g(p->device);
     KORE_TRY(kore_prof_collect(p));
-    IrState irs;
-    KORE_TRY(kore_ir_read(p, &irs));
+    IrState irs{};
+    if (p->d_ir) KORE_TRY(kore_ir_read(p, &irs));
     if (out) {
         const double e = p->factor_elt ? (double)p->factor_elt : 16.0;
         const double S = p->S, K = p->K, np = (double)p->np;

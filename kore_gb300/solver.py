@@ -84,6 +84,18 @@ class Pencil:
         self.sigma, self.precision = sigma, precision
         return self
 
+    def factor_shifts(self, sigmas, precision="fp64"):
+        """Factorise A - sigma_s B for every shift at once (batched kernels); then
+        ``solve`` takes an (n, k * nshift) array whose column j uses shift j % nshift."""
+        sig = np.ascontiguousarray(np.asarray(sigmas, dtype=np.complex128).ravel())
+        t = time.perf_counter()
+        L.check(self.lib.kore_factor_shifts(self._plan, len(sig), L.ptr(sig.view(np.float64)), L.PREC[precision]),
+                "kore_factor_shifts")
+        self.factor_s = time.perf_counter() - t
+        self.sigma = complex(sig[0]) if len(sig) == 1 else tuple(sig)
+        self.precision = precision
+        return self
+
     def solve(self, b, refine_tol=0.0, stats=False):
         """x = (A - sigma B)^-1 b for a vector or the columns of an (n, k) array."""
         b = np.asarray(b)
