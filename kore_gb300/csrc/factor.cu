@@ -109,6 +109,27 @@ __global__ void k_rowinfo(FV<C> v, double *__restrict__ red) {
     }
 }
 
+// Values of the padded level-0 coupling rows for every shift: rscale_row * A entry in
+// the factor precision (grid (x, shift)).
+template <typename C>
+__global__ void k_ell_fill(int64_t ell_stride, int ell_w, int ntile, int S, int64_t np,
+                           const int *__restrict__ src, const double2 *__restrict__ aval,
+                           const double *__restrict__ rscale, C *__restrict__ val) {
+    const int64_t s = blockIdx.y;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < ell_stride;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int e = src[idx];
+        C v = czero<C>();
+        if (e >= 0) {
+            const int64_t lane = idx & 31, tile = idx / 32 / ell_w;   // tile = bi * ntile + t
+            const int64_t bi = tile / ntile, t = tile - bi * ntile;
+            const int64_t row = 2 * bi * S + t * 32 + lane;
+            v = from_c128<C>(rscale[s * np + row] * aval[e]);
+        }
+        val[s * ell_stride + idx] = v;
+    }
+}
+
 // Dw <- 0 with the identity on the padded diagonal of every block, all shifts.
 template <typename C>
 __global__ void k_Dw_init(FV<C> v, int nshift) {
@@ -626,7 +647,7 @@ int ensure_factor_storage(kore_plan *p, int cap, size_t elt) {
                      (void **)&p->d_rscale, (void **)&p->d_piv, (void **)&p->d_pidx, (void **)&p->d_used,
                      (void **)&p->d_sigma, (void **)&p->d_minf, (void **)&p->d_bb, (void **)&p->d_xb, (void **)&p->d_rb,
                      (void **)&p->d_bn, (void **)&p->d_rn, (void **)&p->d_part, (void **)&p->d_ir,
-                     (void **)&p->d_cnt};
+                     (void **)&p->d_cnt, &p->d_ell_val};
     for (void **b : bufs) {
         if (*b) cudaFree(*b);
         *b = nullptr;
@@ -657,9 +678,11 @@ int ensure_factor_storage(kore_plan *p, int cap, size_t elt) {
     KORE_TRY(kore_alloc(p, (void **)&p->d_rb, c * p->np * sizeof(double2)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_bn, c * sizeof(double)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_rn, c * sizeof(double)));
-    KORE_TRY(kore_alloc(p, (void **)&p->d_part, c * 2 * (size_t)kore_div_up(p->np * 16, 256) * sizeof(double)));
+    // per-CTA maxima of the residual products: (np / 64 + np / 8 + 2) CTAs at most, 2 each
+    KORE_TRY(kore_alloc(p, (void **)&p->d_part, c * 2 * (size_t)(p->np / 64 + p->np / 8 + 1024) * sizeof(double)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_ir, c * sizeof(IrState)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_cnt, c * (size_t)(3 * p->nlev + 1) * p->K * sizeof(int)));
+    KORE_TRY(kore_alloc(p, &p->d_ell_val, c * std::max<int64_t>(p->ell_stride(), 1) * elt));
     KORE_CUDA_TRY(cudaMemset(p->d_LU, 0, c * p->lu_stride() * elt));
     KORE_CUDA_TRY(cudaMemset(p->d_piv, 0, c * p->p_stride() * sizeof(int)));
     KORE_CUDA_TRY(cudaMemset(p->d_pidx, 0xff, c * p->p_stride() * sizeof(int)));
@@ -694,13 +717,21 @@ int kore_factor_impl(kore_plan *p, int nshift, const double *sigmas, int precisi
     int s;
     if (precision == KORE_PREC_FP64) {
         k_rowinfo<double2><<<dim3(grid, nshift), 256, 0, p->stream>>>(make_fv<double2>(p), d_red);
-        KORE_LAUNCHED(1);
+        if (p->ell_stride() > 0)
+            k_ell_fill<double2><<<dim3(std::min<unsigned>(kore_div_up(p->ell_stride(), 256), 4096u), nshift), 256, 0,
+                              p->stream>>>(p->ell_stride(), p->ell_w, (p->S + 31) / 32, p->S, p->np, p->d_ell_src,
+                                           p->d_aval, p->d_rscale, static_cast<double2 *>(p->d_ell_val));
+        KORE_LAUNCHED(2);
         KORE_CUDA_TRY(cudaMemcpyAsync(red.data(), d_red, red.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
         KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
         s = factor_dispatch<double2>(p);
     } else {
         k_rowinfo<float2><<<dim3(grid, nshift), 256, 0, p->stream>>>(make_fv<float2>(p), d_red);
-        KORE_LAUNCHED(1);
+        if (p->ell_stride() > 0)
+            k_ell_fill<float2><<<dim3(std::min<unsigned>(kore_div_up(p->ell_stride(), 256), 4096u), nshift), 256, 0,
+                              p->stream>>>(p->ell_stride(), p->ell_w, (p->S + 31) / 32, p->S, p->np, p->d_ell_src,
+                                           p->d_aval, p->d_rscale, static_cast<float2 *>(p->d_ell_val));
+        KORE_LAUNCHED(2);
         KORE_CUDA_TRY(cudaMemcpyAsync(red.data(), d_red, red.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
         KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
         s = factor_dispatch<float2>(p);

@@ -31,9 +31,13 @@ struct BcrLevel {
     int64_t lu_nL, lu_nU;      // next level's couplings (-1 when the next level is the top)
 };
 
+// Rows with more stored values (split A + B) than this are given a whole warp in the
+// sparse products (the dense tau-method boundary rows); the others get 4 lanes.
+constexpr int kKoreLongRow = 128;
+
 // The pencil is stored l-major and padded: block i (of nblocks K) occupies padded
-// slots [i*S, (i+1)*S) where S is the largest block size; slots past the block's
-// own size are identity rows/columns with zero right-hand side.
+// slots [i*S, (i+1)*S) where S is the largest block size rounded up to a multiple of 4;
+// slots past the block's own size are identity rows/columns with zero right-hand side.
 struct kore_plan {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -54,6 +58,15 @@ struct kore_plan {
     int64_t b_nnz = 0;
     bool has_b = false;
     int64_t *d_slot2orig = nullptr;   // np: original index or -1 for a pad slot
+    // A for the sparse products, as a real matrix: row p holds the entries with a
+    // nonzero real part (value Re a) in [srow[p], smid[p]) and those with a nonzero
+    // imaginary part (value Im a) in [smid[p], srow[p+1]), so A x costs two real
+    // multiply-adds per stored value (most entries of A are real or imaginary)
+    int *d_srow = nullptr, *d_smid = nullptr, *d_scol = nullptr;
+    double *d_sval = nullptr;
+    int64_t s_nnz = 0;
+    int *d_long_rows = nullptr;       // rows with more than kKoreLongRow stored values (A + B): a warp each
+    int nlong = 0;
     int *d_bsz = nullptr;             // K
 
     // factorisation: block cyclic reduction (factor.cu).  Level l has lev[l].Kl active
@@ -82,11 +95,21 @@ struct kore_plan {
     int *d_piv = nullptr;             // nodd_max x S per shift: pivot row chosen for column k
     int *d_pidx = nullptr;            // nodd_max x S per shift: position of a row in the current panel or -1
     int *d_used = nullptr;            // nodd_max x S per shift: row already used as a pivot
+    // Level-0 couplings of the even blocks (the rows that the first reduction updates
+    // from the CSR) as padded rows, tile by tile: entry k of row r of tile (bi, t) at
+    // ((bi * ntile + t) * ell_w + k) * 32 + r % 32, ntile = ceil(S / 32).
+    int ell_w = 0;                    // padded width (multiple of 8) of a coupling row
+    int64_t ell_rows = 0;             // even blocks of level 0 x ntile x 32
+    int64_t ell_nnz = 0;              // coupling entries (without the padding)
+    int *d_ell_col = nullptr;         // padded slot of the coupled unknown, -1 for padding
+    int *d_ell_src = nullptr;         // entry of A in the permuted CSR, -1 for padding
+    void *d_ell_val = nullptr;        // per shift: rscale_row * A entry, factor precision
 
     int64_t f_stride() const { return (int64_t)K * S * S; }
     int64_t lu_stride() const { return lu_mats * (int64_t)S * S; }
     int64_t t_stride() const { return (int64_t)nodd_max * 4 * S * S; }
     int64_t p_stride() const { return (int64_t)nodd_max * S; }
+    int64_t ell_stride() const { return ell_rows * ell_w; }
 
     // solve workspace (padded, complex128 unless noted)
     double2 *d_v[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -111,7 +134,6 @@ struct kore_plan {
 
     size_t bytes = 0;
     size_t factor_bytes = 0;          // bytes of the per-shift buffers
-    int sweep_occ[2] = {0, 0};        // co-resident sweep CTAs per SM (complex64, complex128)
     int last_refine_iters = 0;
     double last_resid = 0;
 

@@ -96,7 +96,9 @@ void free_plan(kore_plan *p) {
                     p->d_slot2orig, p->d_bsz, p->d_Dinv, p->d_Gm, p->d_Hm, p->d_Dw, p->d_LU, p->d_lev,
                     p->d_rscale, p->d_T, p->d_piv, p->d_pidx, p->d_used, p->d_zlo, p->d_xlo, p->d_flo,
                     p->d_red, p->d_part, p->d_err, p->d_bar, p->d_ir, p->d_V, p->d_Vtmp, p->d_small,
-                    p->d_sigma, p->d_minf, p->d_bb, p->d_xb, p->d_rb, p->d_bn, p->d_rn, p->d_cnt};
+                    p->d_sigma, p->d_minf, p->d_bb, p->d_xb, p->d_rb, p->d_bn, p->d_rn, p->d_cnt,
+                    p->d_ell_col, p->d_ell_src, p->d_ell_val, p->d_long_rows, p->d_srow, p->d_smid,
+                    p->d_scol, p->d_sval};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     for (auto &v : p->d_v)
@@ -155,6 +157,40 @@ int permute_csr(const kore_plan *p, const std::vector<int64_t> &orig2slot, const
     return bad ? KORE_EINVAL : KORE_OK;
 }
 
+// Padded coupling rows of the level-0 even blocks (kore_plan::d_ell_*) from the
+// permuted CSR of A: the entries left of the diagonal block, then those right of it.
+int build_ell(kore_plan *p, const std::vector<int> &row, const std::vector<int> &col, const std::vector<int> &split) {
+    const int64_t S = p->S;
+    const int nt = (int)((S + 31) / 32);
+    const int64_t ne = p->nlev > 0 ? p->lev[0].neven : 0;
+    int w = 1;
+    for (int64_t bi = 0; bi < ne; ++bi)
+        for (int64_t r = 0; r < S; ++r) {
+            const int64_t q = 2 * bi * S + r;
+            w = std::max(w, (split[2 * q] - row[q]) + (row[q + 1] - split[2 * q + 1]));
+        }
+    p->ell_w = (w + 7) & ~7;
+    p->ell_rows = ne * nt * 32;
+    std::vector<int> ecol(std::max<int64_t>(p->ell_stride(), 1), -1), esrc(ecol.size(), -1);
+    for (int64_t bi = 0; bi < ne; ++bi)
+        for (int64_t r = 0; r < S; ++r) {
+            const int64_t q = 2 * bi * S + r;
+            const int64_t base = ((bi * nt + r / 32) * p->ell_w) * 32 + r % 32;
+            int k = 0;
+            auto put = [&](int e) {
+                ecol[base + (int64_t)k * 32] = col[e];
+                esrc[base + (int64_t)k * 32] = e;
+                ++k;
+            };
+            for (int e = row[q]; e < split[2 * q]; ++e) put(e);
+            for (int e = split[2 * q + 1]; e < row[q + 1]; ++e) put(e);
+            p->ell_nnz += k;
+        }
+    KORE_TRY(upload(p, &p->d_ell_col, ecol));
+    KORE_TRY(upload(p, &p->d_ell_src, esrc));
+    return KORE_OK;
+}
+
 int create(const kore_pencil_desc *d, int device, kore_plan **out) {
     if (!d || !out || d->n <= 0 || d->nblocks <= 0 || !d->block_sizes || !d->perm || !d->a_indptr)
         return KORE_EINVAL;
@@ -172,7 +208,9 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
         p->boff[i + 1] = p->boff[i] + p->bsz[i];
     }
     if (p->boff[p->K] != p->n) return KORE_EINVAL;
-    p->S = *std::max_element(p->bsz.begin(), p->bsz.end());
+    // padded block size: a multiple of 4 so that every factor column (S complex64
+    // entries) starts on a 32-byte boundary, as the tensor-copy sweep needs
+    p->S = (*std::max_element(p->bsz.begin(), p->bsz.end()) + 3) & ~3;
     if (p->S > 1024) return KORE_EINVAL;
     p->np = (int64_t)p->K * p->S;
     if (p->np * 8 >= (int64_t)INT32_MAX) return KORE_EINVAL;
@@ -187,9 +225,11 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
             slot2orig[(int64_t)i * p->S + k] = o;
         }
 
+    kore_build_levels(p);
     KORE_CUDA_TRY(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
     KORE_CUDA_TRY(cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, device));
 
+    std::vector<int> rowlen;
     {
         std::vector<int> row, col, split;
         std::vector<double2> val;
@@ -200,6 +240,28 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
         KORE_TRY(upload(p, &p->d_acol, col));
         KORE_TRY(upload(p, &p->d_aval, val));
         KORE_TRY(upload(p, &p->d_asplit, split));
+        KORE_TRY(build_ell(p, row, col, split));
+        // real/imaginary split of A for the sparse products
+        std::vector<int> srow(p->np + 1, 0), smid(p->np), scol;
+        std::vector<double> sval;
+        scol.reserve(col.size() + col.size() / 2);
+        sval.reserve(col.size() + col.size() / 2);
+        for (int64_t q = 0; q < p->np; ++q) {
+            for (int e = row[q]; e < row[q + 1]; ++e)
+                if (val[e].x != 0.0) { scol.push_back(col[e]); sval.push_back(val[e].x); }
+            smid[q] = (int)scol.size();
+            for (int e = row[q]; e < row[q + 1]; ++e)
+                if (val[e].y != 0.0) { scol.push_back(col[e]); sval.push_back(val[e].y); }
+            srow[q + 1] = (int)scol.size();
+        }
+        if (scol.size() >= (size_t)INT32_MAX) return KORE_EINVAL;
+        p->s_nnz = (int64_t)scol.size();
+        KORE_TRY(upload(p, &p->d_srow, srow));
+        KORE_TRY(upload(p, &p->d_smid, smid));
+        KORE_TRY(upload(p, &p->d_scol, scol));
+        KORE_TRY(upload(p, &p->d_sval, sval));
+        rowlen.resize(p->np);
+        for (int64_t q = 0; q < p->np; ++q) rowlen[q] = srow[q + 1] - srow[q];
     }
     p->has_b = d->b_nnz > 0 && d->b_indptr && d->b_indices && d->b_data;
     if (p->has_b) {
@@ -210,10 +272,19 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
         KORE_TRY(upload(p, &p->d_brow, row));
         KORE_TRY(upload(p, &p->d_bcol, col));
         KORE_TRY(upload(p, &p->d_bval, val));
+        for (int64_t q = 0; q < p->np; ++q) rowlen[q] += row[q + 1] - row[q];
+    }
+    {
+        // rows with more than kKoreLongRow stored values (the sparse products give them a warp each)
+        std::vector<int> longr;
+        for (int64_t q = 0; q < p->np; ++q)
+            if (rowlen[q] > kKoreLongRow) longr.push_back((int)q);
+        p->nlong = (int)longr.size();
+        if (longr.empty()) longr.push_back(0);
+        KORE_TRY(upload(p, &p->d_long_rows, longr));
     }
     KORE_TRY(upload(p, &p->d_slot2orig, slot2orig));
     KORE_TRY(upload(p, &p->d_bsz, p->bsz));
-    kore_build_levels(p);
     if (!p->lev.empty()) {
         KORE_TRY(kore_alloc(p, (void **)&p->d_lev, p->lev.size() * sizeof(BcrLevel)));
         KORE_CUDA_TRY(cudaMemcpy(p->d_lev, p->lev.data(), p->lev.size() * sizeof(BcrLevel), cudaMemcpyHostToDevice));
@@ -362,13 +433,14 @@ int kore_profile(kore_plan *p, int enable, double *out) {
         out[2] = p->prof_ms[1];
         out[3] = (double)p->prof_n[1];
         // one sweep reads every D^-1, G, H block once, the dense couplings of the even
-        // blocks of levels >= 1, the level-0 couplings from the CSR (16 B value + 4 B
-        // index per entry), the right-hand side (16 B) and row scales (8 B) and writes x
-        // (16 B); the reduction vectors f, z, x in factor precision are read and written
-        // about twice each
+        // blocks of levels >= 1, the level-0 couplings of the even blocks (a value in
+        // factor precision + a 4 B index per entry), the right-hand side (16 B) and row
+        // scales (8 B) and writes x (16 B); the reduction vectors f, z, x in factor
+        // precision are read and written about twice each
         double lu = 0.0;
         for (int l = 1; l < p->nlev; ++l) lu += 2.0 * p->lev[l].neven;
-        out[4] = (3.0 * K + lu) * S * S * e + 20.0 * (double)p->a_nnz + np * (16.0 + 8.0 + 16.0) + 6.0 * np * e;
+        out[4] = (3.0 * K + lu) * S * S * e + (double)p->ell_nnz * (e + 4.0) + np * (16.0 + 8.0 + 16.0) +
+                 6.0 * np * e;
         // Gauss-Jordan on [D_j | L_j | U_j | I] for every eliminated block (trailing update
         // 8 S nb (4S - k0 - nb) real flops per panel, ~28 S^3 per block) and four dense
         // S^3 complex products (8 S^3 real flops each) per surviving block of levels >= 1

@@ -8,9 +8,9 @@
 // the last block is solved, x_0 = D_0^-1 f_0, and the levels are unwound in reverse,
 //     level l, odd blocks j:   x_j = z_j - G_j x_jl - H_j x_jr,
 // then x <- s x.  One cooperative persistent kernel runs all phases (about 3 log2 K of
-// them) with a bounded grid barrier between dependent phases; inside a phase every
-// (block, row tile) is independent, so each phase is a batched matrix-vector product
-// streaming the factors from HBM across the whole GPU.
+// them) as a dataflow over tiles of 32 rows: a tile starts as soon as the blocks it
+// reads are complete (per-block completion counters), and the factor blocks stream
+// from HBM through shared memory by TMA.
 //
 // Every kernel here works on all factorised shifts at once (shift s: its own factors,
 // row scales and vectors at offset s * stride), so a batch of forcing frequencies is
@@ -19,83 +19,33 @@
 // In mixed precision the factors are complex64 and the result is refined in FP64:
 //     r = b - (A - sigma B) x,  x += M32^-1 r   until ||r||_inf <= tol (||M||_inf ||x||_inf + ||b||_inf).
 #include "kore_internal.cuh"
+#include "kore_tma.cuh"
 #include <cstddef>
 #include <mutex>
 
 namespace {
 
-constexpr int kSweepWarps = 8;                 // warps of a sweep CTA; they split the columns
-constexpr int kSweepThreads = 32 * kSweepWarps;  // a CTA computes 32 rows of one block
-
 __device__ __forceinline__ double2 ldcg(const double2 *p) { return __ldcg(p); }
 __device__ __forceinline__ float2 ldcg(const float2 *p) { return __ldcg(p); }
+__device__ __forceinline__ double2 ldg(const double2 *p) { return __ldg(p); }
+__device__ __forceinline__ double2 shfl_down_w(double2 v, int o, int width) {
+    v.x = __shfl_down_sync(0xffffffffu, v.x, o, width);
+    v.y = __shfl_down_sync(0xffffffffu, v.y, o, width);
+    return v;
+}
+__device__ __forceinline__ float2 ldg(const float2 *p) { return __ldg(p); }
 __device__ __forceinline__ void stcg(double2 *p, double2 v) { __stcg(p, v); }
 __device__ __forceinline__ void stcg(float2 *p, float2 v) { __stcg(p, v); }
-
-// Rows [r0, r0+32) of M1 v1 (+ M2 v2): lane = row, warp w = column range; column-major
-// S x S blocks so every column read is a coalesced 32-row segment.  The partial sums
-// of the warps are combined through shared memory; the result is returned to the
-// lanes of warp 0 (row r0 + lane).
-template <typename C, int U>
-__device__ __forceinline__ void col_range_dot(const C *__restrict__ M1, const C *__restrict__ v1,
-                                              const C *__restrict__ M2, const C *__restrict__ v2, int S, int r,
-                                              int c0, int c1, C &a0, C &a1) {
-    int c = c0;
-    for (; c + U <= c1; c += U) {
-        C m[U], n[U];
-#pragma unroll
-        for (int t = 0; t < U; ++t) m[t] = __ldg(M1 + r + (int64_t)(c + t) * S);
-        if (M2) {
-#pragma unroll
-            for (int t = 0; t < U; ++t) n[t] = __ldg(M2 + r + (int64_t)(c + t) * S);
-        }
-#pragma unroll
-        for (int t = 0; t < U; ++t) a0 = cfma(a0, m[t], v1[c + t]);
-        if (M2) {
-#pragma unroll
-            for (int t = 0; t < U; ++t) a1 = cfma(a1, n[t], v2[c + t]);
-        }
-    }
-    for (; c < c1; ++c) {
-        a0 = cfma(a0, __ldg(M1 + r + (int64_t)c * S), v1[c]);
-        if (M2) a1 = cfma(a1, __ldg(M2 + r + (int64_t)c * S), v2[c]);
-    }
-}
-
-// Rows [r0, r0+32) of M1 v1 (+ M2 v2): lane = row, warp w = column range; column-major
-// S x S blocks so every column read is a coalesced 32-row segment.  Eight loads are in
-// flight per thread (8 of one matrix, or 4 + 4 of two).  The partial sums of the warps
-// are combined through shared memory; the result is returned to the lanes of warp 0
-// (row r0 + lane).
-template <typename C>
-__device__ __forceinline__ C tile_gemv(const C *__restrict__ M1, const C *__restrict__ v1, const C *__restrict__ M2,
-                                       const C *__restrict__ v2, int S, int r0, C (*red)[33]) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int r = r0 + lane;
-    const int cw = (S + kSweepWarps - 1) / kSweepWarps;
-    const int c0 = w * cw, c1 = min(S, c0 + cw);
-    C a0 = czero<C>(), a1 = czero<C>();
-    if (r < S) {
-        if (M2) col_range_dot<C, 4>(M1, v1, M2, v2, S, r, c0, c1, a0, a1);
-        else col_range_dot<C, 8>(M1, v1, nullptr, nullptr, S, r, c0, c1, a0, a1);
-    }
-    red[w][lane] = a0 + a1;
-    __syncthreads();
-    C out = czero<C>();
-    if (w == 0) {
-#pragma unroll
-        for (int k = 0; k < kSweepWarps; ++k) out = out + red[k][lane];
-    }
-    return out;
-}
 
 struct SweepArgs {
     int K, S, nlev, nshift;
     const BcrLevel *levs;
     const void *Dinv, *G, *H, *LU;
     int64_t f_stride, lu_stride;     // per-shift strides of the factor blocks (elements)
-    const int *arow, *acol, *asplit;
-    const double2 *aval;
+    const int *ell_col;              // level-0 couplings as padded rows (kore_plan::d_ell_*)
+    const void *ell_val;
+    int ell_w;
+    int64_t ell_stride;              // per-shift stride of ell_val (elements)
     const double2 *b;                // nshift x np right-hand sides (complex128, padded)
     const double *rscale;            // nshift x np
     const double *bnorm;             // nshift scalings
@@ -125,8 +75,8 @@ __device__ __forceinline__ void wait_count(const int *c, int target, int *err) {
     __threadfence();   // acquire: the producer's data is read after the counter
 }
 
-// Dataflow sweep.  The tiles (32 rows of one block) of all stages are numbered in a
-// topological order
+// ----------------------------------------------------------------------------- the sweep kernel
+// The tiles (32 rows of one block) of all stages are numbered in a topological order
 //     A_0, B_0, A_1, B_1, ..., A_{L-1}, B_{L-1}, top, C_{L-1}, ..., C_0
 // (A: z_j = D_j^-1 f_j, B: f_i -= L_i z_jl + U_i z_jr, C: x_j = z_j - G_j x_jl - H_j x_jr)
 // and CTA c takes tiles c, c + G, c + 2G, ...  A tile waits only for the counters of
@@ -134,29 +84,130 @@ __device__ __forceinline__ void wait_count(const int *c, int target, int *err) {
 // its rows it adds 1 to the counter of (stage, block).  Tiles are taken in increasing
 // order by co-resident CTAs, so every wait is on a tile of a lower number that some
 // CTA is processing or has processed: no deadlock, and adjacent stages overlap.
+//
+// A tile of A, C, top or B at levels >= 1 reads one or two S x S blocks (stored
+// column-major); they are cut into
+// chunks of 32 rows x kCols columns (16 KB) that one producer thread copies with
+// cp.async.bulk.tensor into a ring of shared-memory slots, each slot guarded by a
+// "full" mbarrier (completed by the copy) and an "empty" mbarrier (one arrival per
+// consumer warp).  The producer runs ahead through the CTA's tile sequence: the factor
+// data of later tiles does not depend on the sweep, so it is fetched while the eight
+// consumer warps wait for their input vectors.  Several hundred KB per SM are in
+// flight without holding registers.  B_0 reads the level-0 couplings as padded rows
+// (at most a few dozen entries per row) with plain coalesced loads instead.
+constexpr int kTmaConsumerWarps = 8;
+constexpr int kTmaConsumers = 32 * kTmaConsumerWarps;
+constexpr int kTmaThreads = kTmaConsumers + 32;   // + one producer warp
+constexpr int kChunkBytes = 16384;
+constexpr int kTileRows = 32;
+constexpr int kMaxRing = 13;
+constexpr int kEllReg = 4;   // level-0 coupling entries per thread held in registers (width 32)
+
+enum { kMapDinv = 0, kMapG = 1, kMapH = 2, kMapLU = 3 };
+
+struct SweepTmaParams {
+    CUtensorMap maps[4];   // Dinv, G, H, LU: (2S reals, S columns, blocks, shifts)
+    SweepArgs a;
+    int nst;               // ring slots
+};
+
+template <typename C> struct TmaShape {
+    static constexpr int kCols = kChunkBytes / (kTileRows * (int)sizeof(C));   // columns per chunk
+    static constexpr int kColsPerWarp = kCols / kTmaConsumerWarps;
+};
+
+// One tile of the sweep: stage kind (0 A, 1 B, 2 top, 3 C), level, shift, block of its
+// rows, first row, and the blocks it multiplies (map, block index within the map).
+struct TileJob {
+    int kind, l, nmat, r0;
+    int64_t s, blk;
+    int map[2];
+    int64_t mblk[2];
+    int64_t vblk[2];     // block of the vector each matrix multiplies
+    bool hasl, hasr;
+};
+
+__device__ __forceinline__ void decode_tile(int64_t g, int &k, const int64_t *st_begin, const BcrLevel *lv_s, int L,
+                                            int ntile, TileJob &t) {
+    while (g >= st_begin[k + 1]) ++k;
+    const int64_t loc = g - st_begin[k];
+    if (k < 2 * L) { t.kind = (k & 1) ? 1 : 0; t.l = k >> 1; }
+    else if (k == 2 * L) { t.kind = 2; t.l = L; }
+    else { t.kind = 3; t.l = L - 1 - (k - 2 * L - 1); }
+    const int nblk = (t.kind == 0 || t.kind == 3) ? lv_s[t.l].nodd : (t.kind == 1 ? lv_s[t.l].neven : 1);
+    t.s = loc / ((int64_t)nblk * ntile);
+    const int64_t rem = loc - t.s * nblk * ntile;
+    const int64_t bi = rem / ntile;
+    t.r0 = (int)(rem - bi * ntile) * kTileRows;
+    t.nmat = 0;
+    t.hasl = t.hasr = false;
+    if (t.kind == 0) {
+        const int64_t j = (2 * bi + 1) * lv_s[t.l].stride;
+        t.blk = j;
+        t.map[0] = kMapDinv; t.mblk[0] = j; t.vblk[0] = j; t.nmat = 1;
+    } else if (t.kind == 1) {
+        const BcrLevel lv = lv_s[t.l];
+        const int64_t q = 2 * bi;
+        t.blk = q * lv.stride;
+        t.hasl = q >= 1;
+        t.hasr = q + 1 < lv.Kl;
+        if (t.l > 0) {
+            // L_q z_jl first when it exists, then U_q z_jr
+            const int64_t jl = (q - 1) * lv.stride, jr = (q + 1) * lv.stride;
+            t.map[0] = t.map[1] = kMapLU;
+            t.mblk[0] = t.hasl ? lv.lu_L + q : lv.lu_U + q;
+            t.vblk[0] = t.hasl ? jl : jr;
+            t.mblk[1] = lv.lu_U + q;
+            t.vblk[1] = jr;
+            t.nmat = (int)t.hasl + (int)t.hasr;
+        }
+    } else if (t.kind == 2) {
+        t.blk = 0;
+        t.map[0] = kMapDinv; t.mblk[0] = 0; t.vblk[0] = 0; t.nmat = 1;
+    } else {
+        const BcrLevel lv = lv_s[t.l];
+        const int64_t q = 2 * bi + 1, j = q * lv.stride;
+        t.blk = j;
+        t.hasr = q + 1 < lv.Kl;
+        t.map[0] = kMapG; t.mblk[0] = j; t.vblk[0] = j - lv.stride; t.nmat = 1;
+        if (t.hasr) { t.map[1] = kMapH; t.mblk[1] = j; t.vblk[1] = j + lv.stride; t.nmat = 2; }
+    }
+}
+
 template <typename C>
-__global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(SweepArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *v1 = reinterpret_cast<C *>(smem_raw);
-    C *v2 = v1 + a.S;
-    __shared__ C red[kSweepWarps][33];
+__global__ void __launch_bounds__(kTmaThreads, 2) k_sweep_tma(const __grid_constant__ SweepTmaParams P) {
+    using Shape = TmaShape<C>;
+    constexpr int kCols = Shape::kCols, kCpw = Shape::kColsPerWarp;
+    const SweepArgs &a = P.a;
+    const int nst = P.nst;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const int S = a.S, ns = a.nshift, L = a.nlev, K = a.K;
+    const int nc = (S + kCols - 1) / kCols;   // chunks per block
+    const int nvec = nc * kCols;
+    unsigned char *ring = smem_raw;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)nst * kChunkBytes);
+    uint64_t *empty = full + nst;
+    C *vbuf = reinterpret_cast<C *>(empty + nst);   // 2 x nvec
+    __shared__ C red[kTmaConsumerWarps][33];
     __shared__ BcrLevel lv_s[kMaxLevels];
     __shared__ int64_t st_begin[3 * kMaxLevels + 2];
-    // uniform over the grid: the flags were set by an earlier kernel
     if (a.skip) {
         bool all = true;
-        for (int s = 0; s < a.nshift; ++s) all = all && (a.skip[s * a.skip_stride] != 0);
+        for (int s = 0; s < ns; ++s) all = all && (a.skip[s * a.skip_stride] != 0);
         if (all) return;
     }
-    if (a.count && blockIdx.x == 0 && threadIdx.x == 0) { atomicAdd(a.count, 1); atomicAdd(a.count_total, 1); }
-    const int S = a.S, ns = a.nshift, L = a.nlev, K = a.K;
-    const int64_t SS = (int64_t)S * S, np = (int64_t)K * S;
-    const int ntile = (S + 31) / 32;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (a.count && blockIdx.x == 0 && tid == 0) { atomicAdd(a.count, 1); atomicAdd(a.count_total, 1); }
+    const int64_t np = (int64_t)K * S;
+    const int ntile = (S + kTileRows - 1) / kTileRows;
     const int nstage = 3 * L + 1;
     if (tid < L) lv_s[tid] = a.levs[tid];
+    if (tid == 0) {
+        for (int i = 0; i < nst; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], kTmaConsumerWarps); }
+        mbar_fence_init();
+    }
+    if (tid == kTmaConsumers) for (int i = 0; i < 4; ++i) tma_prefetch_desc(&P.maps[i]);
     __syncthreads();
-    // stage k: 0..2L-1 -> A_{k/2} (even k) / B_{k/2} (odd k); 2L -> top; 2L+1+m -> C_{L-1-m}
     if (tid == 0) {
         int64_t acc = 0;
         for (int k = 0; k < nstage; ++k) {
@@ -171,10 +222,41 @@ __global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(SweepArgs a) {
     }
     __syncthreads();
     const int64_t total = st_begin[nstage];
-    // counter of (shift, stage id, block); stage ids: A_l = l, B_l = L + l, top = 2L, C_l = 2L + 1 + l
-    auto ctr = [&](int64_t s, int sid, int64_t blk) -> int * { return a.cnt + ((s * nstage + sid) * K + blk); };
     auto live = [&](int64_t s) -> bool { return !(a.skip && a.skip[s * a.skip_stride] != 0); };
-    auto fac = [&](const void *base, int64_t s) -> const C * { return static_cast<const C *>(base) + s * a.f_stride; };
+
+    if (w == kTmaConsumerWarps) {
+        // ------------------------------------------------------------------ producer
+        if (lane == 0) {
+            uint32_t slot = 0, ph = 0;
+            int k = 0;
+            uint64_t issued = 0;
+            TileJob t;
+            for (int64_t g = blockIdx.x; g < total; g += gridDim.x) {
+                decode_tile(g, k, st_begin, lv_s, L, ntile, t);
+                if (!live(t.s)) continue;
+#pragma unroll
+                for (int m = 0; m < 2; ++m) {
+                    if (m >= t.nmat) break;
+                    for (int ch = 0; ch < nc; ++ch) {
+                        if (!mbar_wait(&empty[slot], ph ^ 1)) atomicCAS(a.err, 0, KORE_DEVERR_FLAG);
+                        mbar_arrive_expect_tx(&full[slot], kChunkBytes);
+                        tma_load_4d(ring + (size_t)slot * kChunkBytes, &P.maps[t.map[m]], &full[slot],
+                                    2 * t.r0, ch * kCols, (int)t.mblk[m], (int)t.s);
+                        ++issued;
+                        if (++slot == (uint32_t)nst) { slot = 0; ph ^= 1; }
+                    }
+                }
+            }
+            // every copy has landed before the CTA may exit (normally already consumed)
+            const uint64_t first = issued > (uint64_t)nst ? issued - nst : 0;
+            for (uint64_t i = first; i < issued; ++i)
+                if (!mbar_wait(&full[i % nst], (uint32_t)((i / nst) & 1))) atomicCAS(a.err, 0, KORE_DEVERR_FLAG);
+        }
+        return;
+    }
+
+    // ---------------------------------------------------------------------- consumers
+    auto ctr = [&](int64_t s, int sid, int64_t blk) -> int * { return a.cnt + ((s * nstage + sid) * K + blk); };
     auto vec = [&](void *base, int64_t s) -> C * { return static_cast<C *>(base) + s * np; };
     auto rhs0 = [&](int64_t s, int64_t p) -> C {
         const double bn = a.bnorm[s];
@@ -188,135 +270,122 @@ __global__ void __launch_bounds__(kSweepThreads, 3) k_sweep(SweepArgs a) {
         double2 *o = a.out + s * np + p;
         *o = a.accumulate ? *o + d : d;
     };
-    // x of block b is final after C of the level that eliminated it (top for block 0)
     auto xready = [&](int64_t s, int64_t blk) -> int * {
         if (blk == 0) return ctr(s, 2 * L, 0);
-        const int lb = __ffsll(blk) - 1;   // block b is odd at level ctz(b)
+        const int lb = __ffsll(blk) - 1;
         return ctr(s, 2 * L + 1 + lb, blk);
     };
-
+    uint32_t slot = 0, ph = 0;
     int k = 0;
+    TileJob t;
     for (int64_t g = blockIdx.x; g < total; g += gridDim.x) {
-        while (g >= st_begin[k + 1]) ++k;
-        const int64_t loc = g - st_begin[k];
-        int kind, l;
-        if (k < 2 * L) { kind = (k & 1) ? 1 : 0; l = k >> 1; }
-        else if (k == 2 * L) { kind = 2; l = L; }
-        else { kind = 3; l = L - 1 - (k - 2 * L - 1); }
-        const int nblk = (kind == 0 || kind == 3) ? lv_s[l].nodd : (kind == 1 ? lv_s[l].neven : 1);
-        const int64_t s = loc / ((int64_t)nblk * ntile);
-        const int64_t rem = loc - s * nblk * ntile;
-        const int64_t bi = rem / ntile;
-        const int r0 = (int)(rem - bi * ntile) * 32;
-        const bool go = live(s);
-        int *done = nullptr;
-        __syncthreads();   // shared vectors of the previous tile are no longer read
-        if (kind == 0) {
-            // ---------------------------------------------- A_l: z_j = Dinv_j f_j
-            const BcrLevel lv = lv_s[l];
-            const int64_t j = (2 * bi + 1) * lv.stride;
-            done = ctr(s, l, j);
-            if (go) {
-                if (l > 0 && tid == 0) wait_count(ctr(s, L + l - 1, j), ntile, a.err);   // f_j from B_{l-1}
-                __syncthreads();
-                const C *f = vec(a.f, s);
-                for (int c = tid; c < S; c += blockDim.x) v1[c] = (l == 0) ? rhs0(s, j * S + c) : ldcg(f + j * S + c);
-                __syncthreads();
-                const C val = tile_gemv<C>(fac(a.Dinv, s) + j * SS, v1, nullptr, nullptr, S, r0, red);
-                if (w == 0 && r0 + lane < S) stcg(vec(a.z, s) + j * S + r0 + lane, val);
+        decode_tile(g, k, st_begin, lv_s, L, ntile, t);
+        const int64_t s = t.s;
+        const int sid = t.kind == 0 ? t.l : (t.kind == 1 ? L + t.l : (t.kind == 2 ? 2 * L : 2 * L + 1 + t.l));
+        int *done = ctr(s, sid, t.blk);
+        named_sync(1, kTmaConsumers);   // vectors of the previous tile are no longer read
+        if (live(s)) {
+            // level-0 couplings (B_0): this thread's padded entries are loaded before the
+            // wait, as they do not depend on the sweep; lane = row, warp w = entries w + 8u
+            const bool ell = t.kind == 1 && t.l == 0;
+            const int64_t ebase = ((t.blk / 2) * ntile + t.r0 / kTileRows) * (int64_t)a.ell_w * 32 + lane;
+            const C *ellv = static_cast<const C *>(a.ell_val) + s * a.ell_stride;
+            int ecol[kEllReg];
+            C eval[kEllReg];
+#pragma unroll
+            for (int u = 0; u < kEllReg; ++u) {
+                const int kk = w + u * kTmaConsumerWarps;
+                const bool in = ell && kk < a.ell_w;
+                ecol[u] = in ? __ldg(a.ell_col + ebase + (int64_t)kk * 32) : -1;
+                eval[u] = in ? ldg(ellv + ebase + (int64_t)kk * 32) : czero<C>();
             }
-        } else if (kind == 1) {
-            // ---------------------------------------------- B_l: f_i -= L_i z_jl + U_i z_jr
-            const BcrLevel lv = lv_s[l];
-            const int64_t q = 2 * bi, i = q * lv.stride;
-            const bool hasl = q >= 1, hasr = q + 1 < lv.Kl;
-            const int64_t jl = (q - 1) * lv.stride, jr = (q + 1) * lv.stride;
-            done = ctr(s, L + l, i);
-            if (go) {
-                if (tid == 0) {
-                    if (hasl) wait_count(ctr(s, l, jl), ntile, a.err);
-                    if (hasr) wait_count(ctr(s, l, jr), ntile, a.err);
-                    if (l > 0) wait_count(ctr(s, L + l - 1, i), ntile, a.err);   // f_i from B_{l-1}
-                }
-                __syncthreads();
-                const C *z = vec(a.z, s);
-                C *f = vec(a.f, s);
-                if (l == 0) {
-                    // couplings from the CSR: warp w handles rows r0 + 4w .. r0 + 4w + 3
-                    for (int rr = 0; rr < 4; ++rr) {
-                        const int r = r0 + 4 * w + rr;
-                        if (r >= S) break;
-                        const int64_t p = i * S + r;
-                        const double rs = a.rscale[s * np + p];
-                        C acc = czero<C>();
-                        if (hasl)
-                            for (int e = a.arow[p] + lane; e < a.asplit[2 * p]; e += 32)
-                                acc = cfma(acc, from_c128<C>(rs * a.aval[e]), ldcg(z + a.acol[e]));
-                        if (hasr)
-                            for (int e = a.asplit[2 * p + 1] + lane; e < a.arow[p + 1]; e += 32)
-                                acc = cfma(acc, from_c128<C>(rs * a.aval[e]), ldcg(z + a.acol[e]));
-                        acc = warp_sum(acc);
-                        if (lane == 0) stcg(f + p, rhs0(s, p) - acc);
-                    }
+            if (tid == 0) {
+                if (t.kind == 0) {
+                    if (t.l > 0) wait_count(ctr(s, L + t.l - 1, t.blk), ntile, a.err);
+                } else if (t.kind == 1) {
+                    const int64_t st = lv_s[t.l].stride;
+                    if (t.hasl) wait_count(ctr(s, t.l, t.blk - st), ntile, a.err);
+                    if (t.hasr) wait_count(ctr(s, t.l, t.blk + st), ntile, a.err);
+                    if (t.l > 0) wait_count(ctr(s, L + t.l - 1, t.blk), ntile, a.err);
+                } else if (t.kind == 2) {
+                    if (L > 0) wait_count(ctr(s, 2 * L - 1, 0), ntile, a.err);
                 } else {
-                    const C *LU = static_cast<const C *>(a.LU) + s * a.lu_stride;
-                    for (int c = tid; c < S; c += blockDim.x) {
-                        v1[c] = hasl ? ldcg(z + jl * S + c) : czero<C>();
-                        v2[c] = hasr ? ldcg(z + jr * S + c) : czero<C>();
-                    }
-                    __syncthreads();
-                    const C *M1 = hasl ? LU + (lv.lu_L + q) * SS : (hasr ? LU + (lv.lu_U + q) * SS : nullptr);
-                    const C *V1 = hasl ? v1 : v2;
-                    const C *M2 = (hasl && hasr) ? LU + (lv.lu_U + q) * SS : nullptr;
-                    C acc = czero<C>();
-                    if (M1) acc = tile_gemv<C>(M1, V1, M2, v2, S, r0, red);
-                    if (w == 0 && r0 + lane < S) {
-                        const int64_t p = i * S + r0 + lane;
-                        stcg(f + p, ldcg(f + p) - acc);
-                    }
+                    wait_count(xready(s, t.vblk[0]), ntile, a.err);
+                    if (t.nmat > 1) wait_count(xready(s, t.vblk[1]), ntile, a.err);
                 }
             }
-        } else if (kind == 2) {
-            // ---------------------------------------------- top: x_0 = Dinv_0 f_0
-            done = ctr(s, 2 * L, 0);
-            if (go) {
-                if (L > 0 && tid == 0) wait_count(ctr(s, 2 * L - 1, 0), ntile, a.err);   // f_0 from B_{L-1}
-                __syncthreads();
-                const C *f = vec(a.f, s);
-                for (int c = tid; c < S; c += blockDim.x) v1[c] = (L == 0) ? rhs0(s, c) : ldcg(f + c);
-                __syncthreads();
-                const C val = tile_gemv<C>(fac(a.Dinv, s), v1, nullptr, nullptr, S, r0, red);
-                if (w == 0 && r0 + lane < S) emit(s, r0 + lane, val);
-            }
-        } else {
-            // ---------------------------------------------- C_l: x_j = z_j - G_j x_jl - H_j x_jr
-            const BcrLevel lv = lv_s[l];
-            const int64_t q = 2 * bi + 1, j = q * lv.stride;
-            const bool hasr = q + 1 < lv.Kl;
-            const int64_t jl = j - lv.stride, jr = j + lv.stride;
-            done = ctr(s, 2 * L + 1 + l, j);
-            if (go) {
-                if (tid == 0) {
-                    wait_count(xready(s, jl), ntile, a.err);
-                    if (hasr) wait_count(xready(s, jr), ntile, a.err);
+            named_sync(1, kTmaConsumers);
+            if (ell) {
+                const C *z = vec(a.z, s);
+                C acc = czero<C>();
+#pragma unroll
+                for (int u = 0; u < kEllReg; ++u)
+                    if (ecol[u] >= 0) acc = cfma(acc, eval[u], ldcg(z + ecol[u]));
+                for (int kk = w + kEllReg * kTmaConsumerWarps; kk < a.ell_w; kk += kTmaConsumerWarps) {
+                    const int c = __ldg(a.ell_col + ebase + (int64_t)kk * 32);
+                    if (c >= 0) acc = cfma(acc, ldg(ellv + ebase + (int64_t)kk * 32), ldcg(z + c));
                 }
-                __syncthreads();
-                const C *x = vec(a.x, s), *z = vec(a.z, s);
-                for (int c = tid; c < S; c += blockDim.x) {
-                    v1[c] = ldcg(x + jl * S + c);
-                    v2[c] = hasr ? ldcg(x + jr * S + c) : czero<C>();
+                red[w][lane] = acc;
+                named_sync(1, kTmaConsumers);
+                if (w == 0) {
+                    C val = czero<C>();
+#pragma unroll
+                    for (int q = 0; q < kTmaConsumerWarps; ++q) val = val + red[q][lane];
+                    const int r = t.r0 + lane;
+                    if (r < S) {
+                        const int64_t p = t.blk * S + r;
+                        stcg(vec(a.f, s) + p, rhs0(s, p) - val);
+                    }
                 }
-                __syncthreads();
-                const C acc = tile_gemv<C>(fac(a.G, s) + j * SS, v1, hasr ? fac(a.H, s) + j * SS : nullptr, v2, S,
-                                           r0, red);
-                if (w == 0 && r0 + lane < S) {
-                    const int64_t p = j * S + r0 + lane;
-                    emit(s, p, ldcg(z + p) - acc);
+            } else if (t.nmat > 0) {
+                // input vectors (zero past S: the chunk columns past S are zero too)
+                const C *src = (t.kind == 0 || t.kind == 2) ? vec(a.f, s) : (t.kind == 1 ? vec(a.z, s) : vec(a.x, s));
+                const bool from_b = (t.kind == 0 && t.l == 0) || (t.kind == 2 && L == 0);
+#pragma unroll
+                for (int m = 0; m < 2; ++m) {
+                    if (m >= t.nmat) break;
+                    for (int c = tid; c < nvec; c += kTmaConsumers) {
+                        C v = czero<C>();
+                        if (c < S) v = from_b ? rhs0(s, t.vblk[m] * S + c) : ldcg(src + t.vblk[m] * S + c);
+                        vbuf[m * nvec + c] = v;
+                    }
+                }
+                named_sync(1, kTmaConsumers);
+                C acc = czero<C>();
+#pragma unroll
+                for (int m = 0; m < 2; ++m) {
+                    if (m >= t.nmat) break;
+                    const C *vv = vbuf + m * nvec + w * kCpw;
+                    for (int ch = 0; ch < nc; ++ch) {
+                        if (!mbar_wait(&full[slot], ph)) atomicCAS(a.err, 0, KORE_DEVERR_FLAG);
+                        const C *bc = reinterpret_cast<const C *>(ring + (size_t)slot * kChunkBytes) +
+                                      w * kCpw * kTileRows + lane;
+                        const C *vc = vv + ch * kCols;
+#pragma unroll
+                        for (int u = 0; u < kCpw; ++u) acc = cfma(acc, bc[u * kTileRows], vc[u]);
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&empty[slot]);
+                        if (++slot == (uint32_t)nst) { slot = 0; ph ^= 1; }
+                    }
+                }
+                red[w][lane] = acc;
+                named_sync(1, kTmaConsumers);
+                if (w == 0) {
+                    C val = czero<C>();
+#pragma unroll
+                    for (int q = 0; q < kTmaConsumerWarps; ++q) val = val + red[q][lane];
+                    const int r = t.r0 + lane;
+                    if (r < S) {
+                        const int64_t p = t.blk * S + r;
+                        if (t.kind == 0) stcg(vec(a.z, s) + p, val);
+                        else if (t.kind == 1) stcg(vec(a.f, s) + p, ldcg(vec(a.f, s) + p) - val);
+                        else if (t.kind == 2) emit(s, p, val);
+                        else emit(s, p, ldcg(vec(a.z, s) + p) - val);
+                    }
                 }
             }
         }
-        // publish: every write of the tile happens before the counter increment
-        __syncthreads();
+        named_sync(1, kTmaConsumers);
         if (tid == 0) {
             __threadfence();
             atomicAdd(done, 1);
@@ -359,64 +428,126 @@ __global__ void k_reduce_max(const double *__restrict__ in, int n, double *__res
     }
 }
 
-// 4 lanes per row (measured fastest on this structure: each lane keeps ~10 independent
-// gathers in flight), grid-stride over the rows; shift = blockIdx.y (vectors at s * np).
-// mode 0: y = B x.  mode 1: y = A x - lam B x.  mode 2: y = b - (A x - lam B x), and
-// per-CTA maxima of |y| and |x| into part[s * 2 gridDim.x + 2 blockIdx.x (+1)].
-// lam = sig[s] when sig is given.
+// Sparse products y = B x, A x - lam B x and the refinement residual b - (A x - lam B x).
+// On this GPU the FP64 pipe, not HBM, bounds them (about one FP64 multiply-add per
+// SM per clock), so A is stored as a real matrix split into real and imaginary
+// coefficients (two multiply-adds per value instead of four for a complex entry),
+// each row's real and imaginary segments summed separately and combined at the end.
+// Rows are short (a few dozen values): 4 lanes per row, each lane with kRowUnroll
+// gathers in flight.  The tau-method boundary rows are dense over a radial expansion
+// (hundreds of entries); rows with more than kKoreLongRow values (A + B) are listed at plan
+// creation and done by a whole warp each in extra CTAs at the end of the grid, so that
+// they do not hold back the CTAs of the short rows.
 constexpr int kRowLanes = 4;
-__global__ void __launch_bounds__(256) k_spmv(int64_t np, int mode, const int *__restrict__ arow,
-                                              const int *__restrict__ acol, const double2 *__restrict__ aval,
-                                              const int *__restrict__ brow, const int *__restrict__ bcol,
-                                              const double *__restrict__ bval, int has_b, double lre, double lim,
-                                              const double2 *__restrict__ sig, const double2 *__restrict__ x,
-                                              const double2 *__restrict__ rhs, double2 *__restrict__ y,
-                                              double *__restrict__ part, const int *__restrict__ skip,
-                                              int skip_stride) {
-    const int64_t s = blockIdx.y;
-    if (skip && skip[s * skip_stride]) return;
-    x += s * np;
-    y += s * np;
-    if (rhs) rhs += s * np;
-    const int sub = threadIdx.x & (kRowLanes - 1);
-    const int64_t row0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kRowLanes;
-    const int64_t rstride = ((int64_t)gridDim.x * blockDim.x) / kRowLanes;
-    const int64_t nrow_iter = (np + rstride - 1) / rstride;   // same trip count for every lane
-    const double2 lam = sig ? sig[s] : mk(lre, lim);
-    double rmax = 0.0, xmax = 0.0;
-    for (int64_t t = 0; t < nrow_iter; ++t) {
-        const int64_t p = row0 + t * rstride;
-        const bool live = p < np;
-        double2 sa = mk(0.0, 0.0), sb = mk(0.0, 0.0);
-        if (live) {
-            if (mode != 0) {
-                const int e1 = arow[p + 1];
-                for (int e = arow[p] + sub; e < e1; e += kRowLanes)
-                    sa = cfma(sa, __ldg(aval + e), __ldg(x + __ldg(acol + e)));
-            }
-            if (has_b) {
-                const int e1 = brow[p + 1];
-                for (int e = brow[p] + sub; e < e1; e += kRowLanes) sb = sb + __ldg(bval + e) * __ldg(x + __ldg(bcol + e));
-            }
+constexpr int kRowUnroll = 4;
+
+struct SpmvArgs {
+    int64_t np;
+    int mode;               // 0: y = B x.  1: y = A x - lam B x.  2: y = b - (A x - lam B x)
+    int has_b;
+    const int *srow, *smid, *scol;  // A split into real and imaginary coefficients (kore_plan::d_s*)
+    const double *sval;
+    const int *brow, *bcol;
+    const double *bval;
+    const int *long_rows;   // rows done by a warp each
+    int nlong;
+    int short_blocks;       // CTAs of the 4-lane part (the long-row CTAs follow)
+    double2 lam;            // shift when sig is null
+    const double2 *sig;     // per-shift shifts (shift = blockIdx.y)
+    const double2 *x, *rhs;
+    double2 *y;
+    double *part;           // mode 2: per-CTA maxima of |y| and |x|, part[s * 2 gridDim.x + 2 blockIdx.x (+1)]
+    const int *skip;        // shift s is skipped when skip[s * skip_stride] != 0
+    int skip_stride;
+};
+
+// acc += sum over the values sub, sub + LANES, ... of [e0, e1) of val[e] x[col[e]]
+// (kRowUnroll loads in flight per lane, two FP64 multiply-adds per value)
+template <int LANES>
+__device__ __forceinline__ void seg_dot(const int *__restrict__ col, const double *__restrict__ val, int e0, int e1,
+                                        int sub, const double2 *__restrict__ x, double2 &acc) {
+    for (int e = e0 + sub; e < e1; e += LANES * kRowUnroll) {
+        int c[kRowUnroll];
+        double v[kRowUnroll];
+#pragma unroll
+        for (int u = 0; u < kRowUnroll; ++u) {
+            const int q = e + u * LANES;
+            c[u] = q < e1 ? __ldg(col + q) : -1;
+            v[u] = q < e1 ? __ldg(val + q) : 0.0;
         }
 #pragma unroll
-        for (int o = kRowLanes / 2; o > 0; o >>= 1) {
-            sa.x += __shfl_down_sync(0xffffffffu, sa.x, o, kRowLanes);
-            sa.y += __shfl_down_sync(0xffffffffu, sa.y, o, kRowLanes);
-            sb.x += __shfl_down_sync(0xffffffffu, sb.x, o, kRowLanes);
-            sb.y += __shfl_down_sync(0xffffffffu, sb.y, o, kRowLanes);
-        }
-        if (live && sub == 0) {
-            double2 v = (mode == 0) ? sb : sa - lam * sb;
-            if (mode == 2) {
-                v = rhs[p] - v;
-                rmax = fmax(rmax, fmax(fabs(v.x), fabs(v.y)));
-                xmax = fmax(xmax, fmax(fabs(x[p].x), fabs(x[p].y)));
+        for (int u = 0; u < kRowUnroll; ++u)
+            if (c[u] >= 0) {
+                const double2 xv = __ldg(x + c[u]);
+                acc.x = fma(v[u], xv.x, acc.x);
+                acc.y = fma(v[u], xv.y, acc.y);
             }
-            y[p] = v;
+    }
+}
+
+// Partial sums of row p: the real-coefficient values of A (sr), its imaginary-coefficient
+// values (si: A x = sr + i si) and B (sb).
+template <int LANES>
+__device__ __forceinline__ void row_dot(const SpmvArgs &a, int64_t p, int sub, const double2 *__restrict__ x,
+                                        double2 &sr, double2 &si, double2 &sb) {
+    if (a.mode != 0) {
+        const int em = a.smid[p];
+        seg_dot<LANES>(a.scol, a.sval, a.srow[p], em, sub, x, sr);
+        seg_dot<LANES>(a.scol, a.sval, em, a.srow[p + 1], sub, x, si);
+    }
+    if (a.has_b) seg_dot<LANES>(a.bcol, a.bval, a.brow[p], a.brow[p + 1], sub, x, sb);
+}
+
+__global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
+    const int64_t s = blockIdx.y;
+    if (a.skip && a.skip[s * a.skip_stride]) return;
+    const int64_t np = a.np;
+    const double2 *x = a.x + s * np;
+    double2 *y = a.y + s * np;
+    const double2 *rhs = a.rhs ? a.rhs + s * np : nullptr;
+    const double2 lam = a.sig ? a.sig[s] : a.lam;
+    double rmax = 0.0, xmax = 0.0;
+    auto finish = [&](int64_t p, double2 sr, double2 si, double2 sb) {
+        const double2 sa = mk(sr.x - si.y, sr.y + si.x);   // A x = sr + i si
+        double2 v = (a.mode == 0) ? sb : sa - lam * sb;
+        if (a.mode == 2) {
+            v = rhs[p] - v;
+            rmax = fmax(rmax, fmax(fabs(v.x), fabs(v.y)));
+            xmax = fmax(xmax, fmax(fabs(x[p].x), fabs(x[p].y)));
+        }
+        y[p] = v;
+    };
+    if ((int)blockIdx.x < a.short_blocks) {
+        const int sub = threadIdx.x & (kRowLanes - 1);
+        const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kRowLanes;
+        bool live = p < np;
+        if (live) {
+            const int len = (a.srow[p + 1] - a.srow[p]) + (a.has_b ? a.brow[p + 1] - a.brow[p] : 0);
+            live = len <= kKoreLongRow;
+        }
+        double2 sr = mk(0.0, 0.0), si = mk(0.0, 0.0), sb = mk(0.0, 0.0);
+        if (live) row_dot<kRowLanes>(a, p, sub, x, sr, si, sb);
+#pragma unroll
+        for (int o = kRowLanes / 2; o > 0; o >>= 1) {
+            sr = sr + shfl_down_w(sr, o, kRowLanes);
+            si = si + shfl_down_w(si, o, kRowLanes);
+            sb = sb + shfl_down_w(sb, o, kRowLanes);
+        }
+        if (live && sub == 0) finish(p, sr, si, sb);
+    } else {
+        const int lane = threadIdx.x & 31;
+        const int wid = (blockIdx.x - a.short_blocks) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+        if (wid < a.nlong) {
+            const int64_t p = a.long_rows[wid];
+            double2 sr = mk(0.0, 0.0), si = mk(0.0, 0.0), sb = mk(0.0, 0.0);
+            row_dot<32>(a, p, lane, x, sr, si, sb);
+            sr = warp_sum(sr);
+            si = warp_sum(si);
+            sb = warp_sum(sb);
+            if (lane == 0) finish(p, sr, si, sb);
         }
     }
-    if (mode == 2) {
+    if (a.mode == 2) {
         rmax = warp_max_d(rmax);
         xmax = warp_max_d(xmax);
         __shared__ double sm[2][8];
@@ -424,8 +555,8 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t np, int mode, const int *_
         __syncthreads();
         if (threadIdx.x == 0) {
             for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { rmax = fmax(rmax, sm[0][w]); xmax = fmax(xmax, sm[1][w]); }
-            part[s * 2 * gridDim.x + 2 * blockIdx.x] = rmax;
-            part[s * 2 * gridDim.x + 2 * blockIdx.x + 1] = xmax;
+            a.part[s * 2 * gridDim.x + 2 * blockIdx.x] = rmax;
+            a.part[s * 2 * gridDim.x + 2 * blockIdx.x + 1] = xmax;
         }
     }
 }
@@ -448,47 +579,79 @@ __global__ void k_scatter(int64_t np, int64_t n, const int64_t *__restrict__ s2o
     }
 }
 
-template <typename C>
-int occupancy(kore_plan *p, size_t smem) {
-    const int ti = (sizeof(C) == 16) ? 1 : 0;
-    if (p->sweep_occ[ti] == 0) {
-        auto kern = k_sweep<C>;
-        if (smem > 48 * 1024)
-            KORE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        int occ = 0;
-        KORE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kSweepThreads, smem));
-        p->sweep_occ[ti] = std::max(1, std::min(occ, 4));
-    }
-    return KORE_OK;
-}
+// Ring slots and CTAs per SM of the tensor-copy sweep: two CTAs of six 16 KB slots
+// each keep ~200 KB per SM in flight and let one CTA compute while the other waits
+// for its inputs.
+constexpr int kTmaCtasPerSm = 2;
 
 template <typename C>
-int launch_sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int accumulate, const int *skip) {
+size_t tma_smem(int S, int nst) {
+    const int kCols = TmaShape<C>::kCols;
+    const int nvec = ((S + kCols - 1) / kCols) * kCols;
+    return (size_t)nst * kChunkBytes + 2 * (size_t)nst * sizeof(uint64_t) + 2 * (size_t)nvec * sizeof(C);
+}
+
+// Sweep arguments of the plan's factors for `nshift` shifts starting at shift 0; the
+// caller sets the vectors, counters and flags.
+SweepArgs sweep_args(const kore_plan *p, int nshift) {
     SweepArgs a;
-    a.K = p->K; a.S = p->S; a.nlev = p->nlev; a.nshift = p->nshift; a.levs = p->d_lev;
+    a.K = p->K; a.S = p->S; a.nlev = p->nlev; a.nshift = nshift; a.levs = p->d_lev;
     a.Dinv = p->d_Dinv; a.G = p->d_Gm; a.H = p->d_Hm; a.LU = p->d_LU;
     a.f_stride = p->f_stride(); a.lu_stride = p->lu_stride();
-    a.arow = p->d_arow; a.acol = p->d_acol; a.asplit = p->d_asplit; a.aval = p->d_aval;
-    a.b = b; a.rscale = p->d_rscale; a.bnorm = bnorm;
-    a.f = p->d_flo; a.z = p->d_zlo; a.x = p->d_xlo;
-    a.out = x; a.accumulate = accumulate; a.cnt = p->d_cnt; a.err = p->d_err;
-    a.skip = skip; a.skip_stride = (int)(sizeof(IrState) / sizeof(int));
-    a.count = &p->d_ir->sweeps; a.count_total = &p->d_ir->sweeps_total;
-    const size_t smem = 2 * (size_t)p->S * sizeof(C);
-    KORE_TRY(occupancy<C>(p, smem));
-    const int occ = p->sweep_occ[sizeof(C) == 16 ? 1 : 0];
-    KORE_CUDA_TRY(cudaMemsetAsync(p->d_cnt, 0, (size_t)p->nshift * (3 * p->nlev + 1) * p->K * sizeof(int), p->stream));
-    void *args[] = {&a};
-    dim3 grid(p->num_sms * occ), block(kSweepThreads);
-    KORE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_sweep<C>, grid, block, args, smem, p->stream));
+    a.ell_col = p->d_ell_col; a.ell_val = p->d_ell_val; a.ell_w = p->ell_w; a.ell_stride = p->ell_stride();
+    a.rscale = p->d_rscale;
+    return a;
+}
+
+// Tensor maps, ring depth and the cooperative launch of k_sweep_tma; the completion
+// counters a.cnt are zeroed first.
+template <typename C>
+int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st) {
+    SweepTmaParams P;
+    P.a = a;
+    const int rb = (int)sizeof(C) / 2;
+    const int kCols = TmaShape<C>::kCols;
+    const int ns = a.nshift;
+    KORE_TRY(kore_encode_block_map(&P.maps[kMapDinv], p->d_Dinv, rb, p->S, p->K, ns, p->f_stride(), kTileRows, kCols));
+    KORE_TRY(kore_encode_block_map(&P.maps[kMapG], p->d_Gm, rb, p->S, p->K, ns, p->f_stride(), kTileRows, kCols));
+    KORE_TRY(kore_encode_block_map(&P.maps[kMapH], p->d_Hm, rb, p->S, p->K, ns, p->f_stride(), kTileRows, kCols));
+    KORE_TRY(kore_encode_block_map(&P.maps[kMapLU], p->d_LU, rb, p->S, p->lu_mats, ns, p->lu_stride(), kTileRows,
+                                   kCols));
+    // ring depth: as many slots as fit kTmaCtasPerSm CTAs in the SM's shared memory
+    int smem_sm = 0, smem_blk = 0;
+    KORE_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, p->device));
+    KORE_CUDA_TRY(cudaDeviceGetAttribute(&smem_blk, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
+    const size_t static_smem = 8 * 1024;   // reduction tile, level table, stage offsets, per-CTA reserve
+    const size_t budget = std::min<size_t>((size_t)smem_sm / kTmaCtasPerSm, (size_t)smem_blk) - static_smem;
+    int nst = kMaxRing;
+    while (nst > 2 && tma_smem<C>(p->S, nst) > budget) --nst;
+    if (tma_smem<C>(p->S, nst) > budget) return KORE_EINVAL;
+    P.nst = nst;
+    const size_t smem = tma_smem<C>(p->S, nst);
+    auto kern = k_sweep_tma<C>;
+    KORE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    KORE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTmaThreads, smem));
+    if (occ < 1) return KORE_EINVAL;
+    occ = std::min(occ, kTmaCtasPerSm);
+    KORE_CUDA_TRY(cudaMemsetAsync(a.cnt, 0, (size_t)ns * (3 * p->nlev + 1) * p->K * sizeof(int), st));
+    void *args[] = {&P};
+    dim3 grid(p->num_sms * occ), block(kTmaThreads);
+    KORE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)kern, grid, block, args, smem, st));
     KORE_LAUNCHED(1);
     return KORE_OK;
 }
 
 int sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int accumulate, const int *skip) {
     if (p->prof) KORE_TRY(kore_prof_mark(p, 0, true));
-    const int s = (p->prec == KORE_PREC_FP64) ? launch_sweep<double2>(p, b, bnorm, x, accumulate, skip)
-                                              : launch_sweep<float2>(p, b, bnorm, x, accumulate, skip);
+    SweepArgs a = sweep_args(p, p->nshift);
+    a.b = b; a.bnorm = bnorm;
+    a.f = p->d_flo; a.z = p->d_zlo; a.x = p->d_xlo;
+    a.out = x; a.accumulate = accumulate; a.cnt = p->d_cnt; a.err = p->d_err;
+    a.skip = skip; a.skip_stride = (int)(sizeof(IrState) / sizeof(int));
+    a.count = &p->d_ir->sweeps; a.count_total = &p->d_ir->sweeps_total;
+    const int s = (p->prec == KORE_PREC_FP64) ? launch_sweep<double2>(p, a, p->stream)
+                                              : launch_sweep<float2>(p, a, p->stream);
     if (p->prof) KORE_TRY(kore_prof_mark(p, 0, false));
     return s;
 }
@@ -505,15 +668,28 @@ int absmax(kore_plan *p, const double2 *v, double *out, double *scratch) {
     return KORE_OK;
 }
 
-unsigned spmv_grid(int64_t np) { return kore_div_up(np * kRowLanes, 256); }
+// CTAs of one sparse product: the 4-lane part, then 8 long rows per CTA
+unsigned spmv_short_blocks(int64_t np) { return kore_div_up(np * kRowLanes, 256); }
+unsigned spmv_grid(const kore_plan *p) { return spmv_short_blocks(p->np) + kore_div_up(p->nlong, 8); }
+
+SpmvArgs spmv_args(const kore_plan *p, int mode, const double2 *x, double2 *y) {
+    SpmvArgs a;
+    a.np = p->np; a.mode = mode; a.has_b = p->has_b ? 1 : 0;
+    a.srow = p->d_srow; a.smid = p->d_smid; a.scol = p->d_scol; a.sval = p->d_sval;
+    a.brow = p->d_brow; a.bcol = p->d_bcol; a.bval = p->d_bval;
+    a.long_rows = p->d_long_rows; a.nlong = p->nlong; a.short_blocks = (int)spmv_short_blocks(p->np);
+    a.lam = mk(0.0, 0.0); a.sig = nullptr;
+    a.x = x; a.rhs = nullptr; a.y = y; a.part = nullptr;
+    a.skip = nullptr; a.skip_stride = 0;
+    return a;
+}
 
 }  // namespace
 
 int kore_spmv_b(kore_plan *p, const double2 *x, double2 *y) {
     if (!p->has_b) return KORE_EINVAL;
     if (p->prof) KORE_TRY(kore_prof_mark(p, 2, true));
-    k_spmv<<<spmv_grid(p->np), 256, 0, p->stream>>>(p->np, 0, p->d_arow, p->d_acol, p->d_aval, p->d_brow, p->d_bcol,
-                                                     p->d_bval, 1, 0.0, 0.0, nullptr, x, nullptr, y, nullptr, nullptr, 0);
+    k_spmv<<<spmv_grid(p), 256, 0, p->stream>>>(spmv_args(p, 0, x, y));
     KORE_LAUNCHED(1);
     if (p->prof) KORE_TRY(kore_prof_mark(p, 2, false));
     KORE_CUDA_TRY(cudaGetLastError());
@@ -521,9 +697,9 @@ int kore_spmv_b(kore_plan *p, const double2 *x, double2 *y) {
 }
 
 int kore_spmv_pencil(kore_plan *p, double lre, double lim, const double2 *x, double2 *y) {
-    k_spmv<<<spmv_grid(p->np), 256, 0, p->stream>>>(p->np, 1, p->d_arow, p->d_acol, p->d_aval, p->d_brow, p->d_bcol,
-                                                     p->d_bval, p->has_b ? 1 : 0, lre, lim, nullptr, x, nullptr, y,
-                                                     nullptr, nullptr, 0);
+    SpmvArgs a = spmv_args(p, 1, x, y);
+    a.lam = mk(lre, lim);
+    k_spmv<<<spmv_grid(p), 256, 0, p->stream>>>(a);
     KORE_LAUNCHED(1);
     KORE_CUDA_TRY(cudaGetLastError());
     return KORE_OK;
@@ -637,12 +813,12 @@ int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol) {
     k_ir_begin<<<1, ns, 0, p->stream>>>(p->d_ir, ns);
     KORE_LAUNCHED(1);
     KORE_TRY(sweep(p, b, bn, x, 0, nullptr));
-    const unsigned grid = spmv_grid(p->np);
+    const unsigned grid = spmv_grid(p);
+    SpmvArgs ra = spmv_args(p, 2, x, p->d_rb);
+    ra.sig = p->d_sigma; ra.rhs = b; ra.part = p->d_part; ra.skip = &p->d_ir->done; ra.skip_stride = skip_stride;
     for (int it = 0; it < kIrMax; ++it) {
         if (p->prof) KORE_TRY(kore_prof_mark(p, 2, true));
-        k_spmv<<<dim3(grid, ns), 256, 0, p->stream>>>(p->np, 2, p->d_arow, p->d_acol, p->d_aval, p->d_brow, p->d_bcol,
-                                                      p->d_bval, p->has_b ? 1 : 0, 0.0, 0.0, p->d_sigma, x, b, p->d_rb,
-                                                      p->d_part, &p->d_ir->done, skip_stride);
+        k_spmv<<<dim3(grid, ns), 256, 0, p->stream>>>(ra);
         k_ir_check<<<ns, 1024, 0, p->stream>>>(p->d_part, (int)grid, bn, p->d_minf, tol, p->d_ir, rn);
         KORE_LAUNCHED(2);
         if (p->prof) KORE_TRY(kore_prof_mark(p, 2, false));
@@ -696,7 +872,7 @@ namespace {
 
 constexpr int64_t kNoAllocMaxNp = 16384;
 constexpr int64_t kNoAllocMaxCnt = 32768;   // sweep completion counters: (3 levels + 1) x blocks
-constexpr int64_t kNoAllocMaxSpmvCta = (kNoAllocMaxNp * kRowLanes + 255) / 256;
+constexpr int64_t kNoAllocMaxSpmvCta = (kNoAllocMaxNp * kRowLanes + 255) / 256 + kNoAllocMaxNp / 8 + 1;
 
 struct NoAllocScratch {
     double2 bp[kNoAllocMaxNp];      // padded right-hand side (complex128)
@@ -739,28 +915,12 @@ int noalloc_scratch(int device, NoAllocScratch **out) {
 template <typename C>
 int noalloc_sweep(kore_plan *p, NoAllocScratch *s, const double2 *b, const double *bnorm, double2 *x, int accumulate,
                   const int *skip, cudaStream_t st) {
-    SweepArgs a;
-    a.K = p->K; a.S = p->S; a.nlev = p->nlev; a.nshift = 1; a.levs = p->d_lev;
-    a.Dinv = p->d_Dinv; a.G = p->d_Gm; a.H = p->d_Hm; a.LU = p->d_LU;   // shift 0
-    a.f_stride = p->f_stride(); a.lu_stride = p->lu_stride();
-    a.arow = p->d_arow; a.acol = p->d_acol; a.asplit = p->d_asplit; a.aval = p->d_aval;
-    a.b = b; a.rscale = p->d_rscale; a.bnorm = bnorm;
+    SweepArgs a = sweep_args(p, 1);   // shift 0
+    a.b = b; a.bnorm = bnorm;
     a.f = s->f; a.z = s->z; a.x = s->x;
     a.out = x; a.accumulate = accumulate; a.cnt = s->cnt; a.err = &s->err;
     a.skip = skip; a.skip_stride = 0; a.count = &s->ir.sweeps; a.count_total = &s->ir.sweeps_total;
-    const size_t smem = 2 * (size_t)p->S * sizeof(C);
-    auto kern = k_sweep<C>;
-    if (smem > 48 * 1024)
-        KORE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int occ = 0;
-    KORE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kSweepThreads, smem));
-    occ = std::max(1, std::min(occ, 4));
-    KORE_CUDA_TRY(cudaMemsetAsync(s->cnt, 0, (size_t)(3 * p->nlev + 1) * p->K * sizeof(int), st));
-    void *args[] = {&a};
-    dim3 grid(p->num_sms * occ), block(kSweepThreads);
-    KORE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)kern, grid, block, args, smem, st));
-    KORE_LAUNCHED(1);
-    return KORE_OK;
+    return launch_sweep<C>(p, a, st);
 }
 
 int noalloc_solve(kore_plan *p, NoAllocScratch *s, const double2 *b_dev, double2 *x_dev, double tol, cudaStream_t st) {
@@ -782,11 +942,11 @@ int noalloc_solve(kore_plan *p, NoAllocScratch *s, const double2 *b_dev, double2
         k_ir_begin<<<1, 1, 0, st>>>(&s->ir, 1);
         KORE_LAUNCHED(1);
         KORE_TRY(noalloc_sweep<float2>(p, s, s->bp, bn, s->xp, 0, nullptr, st));
-        const unsigned grid = kore_div_up(p->np * kRowLanes, 256);
+        const unsigned grid = spmv_grid(p);
+        SpmvArgs ra = spmv_args(p, 2, s->xp, s->r);
+        ra.lam = mk(p->sigma_re, p->sigma_im); ra.rhs = s->bp; ra.part = s->part; ra.skip = &s->ir.done;
         for (int it = 0; it < kIrMax; ++it) {
-            k_spmv<<<grid, 256, 0, st>>>(p->np, 2, p->d_arow, p->d_acol, p->d_aval, p->d_brow, p->d_bcol, p->d_bval,
-                                         p->has_b ? 1 : 0, p->sigma_re, p->sigma_im, nullptr, s->xp, s->bp, s->r,
-                                         s->part, &s->ir.done, 0);
+            k_spmv<<<grid, 256, 0, st>>>(ra);
             k_ir_check<<<1, 1024, 0, st>>>(s->part, (int)grid, bn, p->d_minf, tol, &s->ir, rn);
             KORE_LAUNCHED(2);
             KORE_TRY(noalloc_sweep<float2>(p, s, s->r, rn, s->xp, 1, &s->ir.done, st));
@@ -833,4 +993,47 @@ extern "C" int kore_solve_dev_noalloc(kore_plan *p, const void *b_dev, void *x_d
     }
     if (prev >= 0 && prev != p->device) cudaSetDevice(prev);
     return rc;
+}
+
+// ----------------------------------------------------------------------------- tensor maps
+namespace {
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled_fn() {
+    static EncodeTiledFn fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(f);
+    }();
+    return fn;
+}
+}  // namespace
+
+int kore_encode_block_map(CUtensorMap *map, const void *base, int real_bytes, int S, int64_t nblk, int nshift,
+                          int64_t shift_stride, int box_rows, int box_cols) {
+    EncodeTiledFn fn = encode_tiled_fn();
+    if (!fn) {
+        std::fprintf(stderr, "kore: cuTensorMapEncodeTiled is not available from the driver\n");
+        return KORE_ECUDA;
+    }
+    const cuuint64_t cb = 2 * (cuuint64_t)real_bytes;   // bytes of one complex entry
+    const cuuint64_t dims[4] = {2 * (cuuint64_t)S, (cuuint64_t)S, (cuuint64_t)nblk, (cuuint64_t)nshift};
+    const cuuint64_t strides[3] = {cb * S, cb * S * S, cb * (cuuint64_t)shift_stride};
+    const cuuint32_t box[4] = {2 * (cuuint32_t)box_rows, (cuuint32_t)box_cols, 1, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = fn(map, real_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4,
+                          const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        std::fprintf(stderr, "kore: cuTensorMapEncodeTiled failed (%d): S=%d blocks=%lld shifts=%d\n", (int)r, S,
+                     (long long)nblk, nshift);
+        return KORE_ECUDA;
+    }
+    return KORE_OK;
 }
