@@ -38,7 +38,23 @@ WORKLOADS = {
 }
 
 
+# Batched forced solves (the tidal-forcing sweep): forcing 10 (a boundary forcing whose
+# right-hand side does not depend on the frequency) on the eigen pencil, nfreq
+# frequencies uniform in [-2, 2] solved `group` at a time, then `instances` uneven
+# problems (m, N, lmax, Ek drawn from the sweep's ranges) solved concurrently.
+FORCED = {
+    "forced4": dict(m=2, symm=1, Ek=1e-6, N=240, lmax=301, ricb=0.35, nfreq=512, group=16, instances=16),
+    # small version of the same for quick checks
+    "forced4s": dict(m=2, symm=1, Ek=1e-5, N=96, lmax=61, ricb=0.35, nfreq=64, group=16, instances=4),
+}
+
+
 def describe(w):
+    if w in FORCED:
+        c = FORCED[w]
+        return (f"batched forced solves: hydro shell ricb={c['ricb']} no-slip m={c['m']} symm={c['symm']} "
+                f"Ek={c['Ek']:g} N={c['N']} lmax={c['lmax']}, forcing 10, {c['nfreq']} frequencies in [-2, 2] "
+                f"({c['group']} per batch), plus {c['instances']} uneven instances")
     m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[w]
     return (f"hydro shell ricb={ricb} no-slip m={m} symm={symm} Ek={Ek:g} N={N} lmax={lmax}, "
             f"target {tau.imag:g}i, nev={nev}, which={which}")
@@ -207,13 +223,128 @@ def cpu_baseline(args):
                       f"scaled to the full workload by the block count"}
 
 
+def uneven_instances(count, seed=7):
+    """Uneven forced problems drawn from the sweep's ranges: m in 1..8 (forcing 10 acts on
+    l = m, so m = 0 has no forcing), N even in [64, 320], lmax in [60, 400] with
+    lmax - m + 1 even, Ek log-uniform in [1e-7, 1e-4], one frequency in [-2, 2] each."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        m = int(rng.integers(1, 9))
+        N = 2 * int(rng.integers(32, 161))
+        lmax = int(rng.integers(60, 401))
+        if (lmax - m + 1) % 2:
+            lmax += 1 if lmax < 400 else -1
+        out.append(dict(m=m, symm=1, Ek=float(10 ** rng.uniform(-7, -4)), N=N, lmax=lmax, ricb=0.35,
+                        w=float(rng.uniform(-2, 2))))
+    return out
+
+
+def forced_bench(args, local):
+    """Batched forced solves: forced solves/s, mixed (complex64 batched factorisation +
+    FP64 refinement) against the FP64 GPU path, through the public Python API
+    (kore_gb300.forced_sweep: host right-hand sides in, host solutions out)."""
+    import torch
+    import scipy.sparse as ss
+    from concurrent.futures import ThreadPoolExecutor
+    from kore_gb300 import Pencil, forced_sweep, kernel_launches
+    from kore_gb300 import build as kb
+    from kore_gb300.assembly import forcing_vector, hydro_params, hydro_pencil
+    from kore_gb300.structure import layout_from_params
+    kb.build()
+    torch.cuda.set_device(local)
+    c = FORCED[args.workload]
+    geo = dict(m=c["m"], symm=c["symm"], Ek=c["Ek"], N=c["N"], lmax=c["lmax"], ricb=c["ricb"])
+    Ae, Be, nrm = hydro_pencil(geo["m"], geo["symm"], geo["Ek"], geo["N"], geo["lmax"], geo["ricb"], with_norm=True)
+    b = forcing_vector(geo["m"], geo["symm"], geo["N"], geo["lmax"], geo["ricb"], 10).toarray().ravel()
+    lay = layout_from_params(hydro_params(**geo))
+    p = Pencil(Ae, Be, layout=lay, device=local)
+    om = np.linspace(-2.0, 2.0, c["nfreq"])
+    G = c["group"]
+
+    def resid(x, w):
+        M = (Ae - (1j * w) * Be).tocsr()
+        r = M @ x - b / nrm
+        return np.abs(r).max() / (abs(M).sum(axis=1).max() * np.abs(x).max() + np.abs(b / nrm).max())
+
+    # warm-up: `warmup` batches of the first frequencies
+    for _ in range(max(args.warmup, 1)):
+        forced_sweep(p, om[:G], b, "mixed", G, refine_tol=1e-14, scale=nrm)
+    launches0 = kernel_launches()
+    clocks = ClockSampler(local)
+    with clocks:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        X, gt = forced_sweep(p, om, b, "mixed", G, refine_tol=1e-14, scale=nrm)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = kernel_launches() - launches0
+    sample = np.linspace(0, len(om) - 1, 9).astype(int)
+    res = np.array([resid(X[:, j], om[j]) for j in sample])
+    # FP64 plain path on the first `fp64` batches
+    nb64 = max(1, min(len(gt), args.fp64_steps if args.fp64_steps is not None else 2))
+    t0 = time.perf_counter()
+    X64, gt64 = forced_sweep(p, om[:nb64 * G], b, "fp64", G, scale=nrm)
+    wall64 = time.perf_counter() - t0
+    diff = max(np.linalg.norm(X[:, j] - X64[:, j]) / np.linalg.norm(X64[:, j]) for j in range(0, nb64 * G, 7))
+    n = int(Ae.shape[0])
+    p.close()
+
+    # uneven instances, four plans in flight at once (each plan has its own stream)
+    inst = uneven_instances(c["instances"])
+    built = []
+    for d in inst:
+        A_i, B_i, nrm_i = hydro_pencil(d["m"], 1, d["Ek"], d["N"], d["lmax"], d["ricb"], with_norm=True)
+        b_i = forcing_vector(d["m"], 1, d["N"], d["lmax"], d["ricb"], 10).toarray().ravel()
+        built.append((d, A_i, B_i, nrm_i, b_i))
+
+    def one(item):
+        d, A_i, B_i, nrm_i, b_i = item
+        q = Pencil(A_i, B_i, layout=layout_from_params(hydro_params(d["m"], 1, d["Ek"], d["N"], d["lmax"], d["ricb"])),
+                   device=local)
+        with q:
+            x, _ = forced_sweep(q, [d["w"]], b_i, "mixed", 1, refine_tol=1e-14, scale=nrm_i)
+        M = (A_i - (1j * d["w"]) * B_i).tocsr()
+        r = M @ x[:, 0] - b_i / nrm_i
+        return np.abs(r).max() / (abs(M).sum(axis=1).max() * np.abs(x).max() + np.abs(b_i / nrm_i).max())
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        res_i = list(ex.map(one, built))
+    wall_i = time.perf_counter() - t0
+    value = len(om) / wall
+    hbytes = (len(om) * n * 16, len(om) * n * 16)
+    line = {
+        "metric": "forced solves/s (batched frequency sweep, resid<=1e-10), mixed vs FP64 GPU",
+        "value": value, "unit": "solves/s", "n_gpus": 1, "steps": len(gt), "warmup": max(args.warmup, 1),
+        "ms_per_step": 1e3 * wall / len(gt), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 factor + f64 refinement", "data": "synthetic: pencil assembled from the kore parameters",
+        "config": {"workload": describe(args.workload), "n": n, "blocks": int(lay.nblocks),
+                   "block": int(lay.block_sizes.max()), "batch": G, "l2": "inputs larger than L2",
+                   "parallelism": "replicas x1"},
+        "latency_ms": {"batch_p50": 1e3 * float(np.percentile(gt, 50)), "batch_p99": 1e3 * float(np.percentile(gt, 99))},
+        "max_resid": float(res.max()),
+        "fp64": {"value": nb64 * G / wall64, "unit": "solves/s", "frequencies": nb64 * G,
+                 "max_rel_diff_mixed_vs_fp64": float(diff)},
+        "speedup_vs_fp64": value / (nb64 * G / wall64),
+        "uneven": {"instances": len(inst), "value": len(inst) / wall_i, "unit": "solves/s (plan + factor + solve, "
+                   "4 plans in flight)", "max_resid": float(max(res_i)),
+                   "sizes": [[d["m"], d["N"], d["lmax"], float(f"{d['Ek']:.3g}")] for d in inst]},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": hbytes[0] // len(gt),
+                "d2h_bytes_per_step": hbytes[1] // len(gt)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="shell2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="shell2", choices=sorted(WORKLOADS) + sorted(FORCED))
     ap.add_argument("--fp64-steps", type=int, default=None)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -224,6 +355,10 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         reference_arm(args, rank, world)
+        return
+    if args.workload in FORCED:
+        if rank == 0:
+            forced_bench(args, local)
         return
 
     import torch

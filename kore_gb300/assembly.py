@@ -200,12 +200,15 @@ def boundary_values(x, N, nder, ricb, rcmb=RCMB):
 
 
 def hydro_pencil(m, symm, Ek, N, lmax, ricb=0.35, bci=1, bco=1, forcing=0, forcing_frequency=0.0,
-                 forcing_amplitude_cmb=1.0, forcing_amplitude_icb=0.0, Gaspard=1.0, ViscosD=None):
+                 forcing_amplitude_cmb=1.0, forcing_amplitude_icb=0.0, Gaspard=1.0, ViscosD=None,
+                 with_norm=False):
     """(A, B) as bin/assemble.py writes them for the hydrodynamic shell problem.
 
     forcing == 0: eigenproblem, B is the (sizmat x sizmat) float64 matrix, A and B
-    divided by ||B||_F.  forcing in (7, 9, 10): forced problem, A = i w u + Coriolis -
-    viscous (unnormalised) and B is the (sizmat x 1) forcing column.
+    divided by ||B||_F (with_norm=True also returns that norm).  forcing in (7, 9, 10):
+    forced problem, A = i w u + Coriolis - viscous (unnormalised) and B is the
+    (sizmat x 1) forcing column.  The forced matrix at frequency w is therefore
+    ||B||_F (A_eig - i w B_eig) of the eigen pencil.
     """
     if ricb <= 0:
         raise ValueError("only the spherical shell (ricb > 0) is assembled here")
@@ -330,8 +333,22 @@ def hydro_pencil(m, symm, Ek, N, lmax, ricb=0.35, bci=1, bco=1, forcing=0, forci
         B = ss.bmat([[-u_p, None], [None, -u_t]], format="csr").astype(np.float64)
         B.eliminate_zeros()
         bnorm = ss.linalg.norm(B)
+        if with_norm:
+            return (A / bnorm).tocsr(), (B / bnorm).tocsr(), float(bnorm)
         return (A / bnorm).tocsr(), (B / bnorm).tocsr()
-    # forcing column (bin/assemble.py:279-427)
+    return A, forcing_vector(m, symm, N, lmax, ricb, forcing, forcing_frequency, forcing_amplitude_cmb,
+                             forcing_amplitude_icb, bci, bco)
+
+
+def forcing_vector(m, symm, N, lmax, ricb, forcing, forcing_frequency=0.0, forcing_amplitude_cmb=1.0,
+                   forcing_amplitude_icb=0.0, bci=1, bco=1):
+    """The (sizmat x 1) forcing column of the forced problem (bin/assemble.py:279-427):
+    forcing 10 and 9 are boundary forcings independent of the frequency, forcing 7
+    (libration) is proportional to it."""
+    N1 = radial_size(N, ricb)
+    nb = (lmax - m + 1) // 2
+    lp, lt = ell(m, lmax, symm)
+    n = 2 * nb * N1
     if forcing == 10:
         if symm != 1:
             raise ValueError("forcing 10 needs symm = 1")
@@ -356,8 +373,7 @@ def hydro_pencil(m, symm, Ek, N, lmax, ricb=0.35, bci=1, bco=1, forcing=0, forci
         raise ValueError(f"forcing {forcing} is not assembled here")
     rows = np.arange(pos, pos + 2)
     keep = vals != 0
-    b = ss.csr_matrix((vals[keep].astype(complex), (rows[keep], np.zeros(keep.sum(), int))), shape=(n, 1))
-    return A, b
+    return ss.csr_matrix((vals[keep].astype(complex), (rows[keep], np.zeros(keep.sum(), int))), shape=(n, 1))
 
 
 def hydro_params(m, symm, Ek, N, lmax, ricb=0.35, **kw):

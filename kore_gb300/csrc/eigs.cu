@@ -606,7 +606,7 @@ int kore_eigs_impl(kore_plan *p, const kore_eps_opts *o, double *evals, double *
     KORE_CUDA_TRY(cudaMemsetAsync(c.Hbar, 0, sizeof(double2) * ldh * m, p->stream));
 
     const size_t schur_smem = (size_t)3 * m * m * sizeof(double2);
-    KORE_CUDA_TRY(cudaFuncSetAttribute(k_schur, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)schur_smem));
+    KORE_TRY(kore_allow_max_dyn_smem(k_schur, p->device));
     std::vector<double> h_est(m);
     std::vector<double2> h_theta(m);
     int h_info = 0;

@@ -515,7 +515,7 @@ template <typename C, int NB>
 int gauss_jordan(kore_plan *p, const FV<C> &v, const BcrLevel &lv, int nodd, int top, int nshift) {
     const int S = p->S;
     const size_t smem = (size_t)S * NB * sizeof(C) + (size_t)S * sizeof(int);
-    KORE_CUDA_TRY(cudaFuncSetAttribute(k_panel<C, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    KORE_TRY(kore_allow_max_dyn_smem(k_panel<C, NB>, p->device));
     const int pthreads = std::min(1024, ((S + 31) / 32) * 32);
     for (int k0 = 0; k0 < S; k0 += NB) {
         const int nb = std::min(NB, S - k0);

@@ -155,3 +155,17 @@ extern std::atomic<long long> g_kore_launches;
     do { int _s = (expr); if (_s != KORE_OK) return _s; } while (0)
 
 static inline unsigned kore_div_up(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+// Let a kernel use the device's largest dynamic shared memory.  The attribute is
+// process-wide, so every caller sets the same value: a plan of another size on another
+// host thread cannot lower it between this thread's setting and its launch.
+template <typename K>
+int kore_allow_max_dyn_smem(K kern, int device) {
+    cudaFuncAttributes fa;
+    KORE_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void *)kern));
+    int optin = 0;
+    KORE_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    KORE_CUDA_TRY(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       optin - (int)fa.sharedSizeBytes));
+    return 0;
+}

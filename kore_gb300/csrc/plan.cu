@@ -296,7 +296,9 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
     KORE_CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
     KORE_CUDA_TRY(cudaMemset(p->d_red, 0, 8192 * sizeof(double)));
     KORE_CUDA_TRY(cudaMallocHost(&p->h_red, 8192 * sizeof(double)));
-    KORE_CUDA_TRY(cudaDeviceSynchronize());
+    // the set-up copies and memsets ran on the legacy default stream; plans' own streams
+    // are non-blocking, so this waits for this plan's set-up only
+    KORE_CUDA_TRY(cudaStreamSynchronize(0));
     *out = guard.release();
     return KORE_OK;
 }

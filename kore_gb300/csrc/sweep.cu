@@ -629,7 +629,7 @@ int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st) {
     P.nst = nst;
     const size_t smem = tma_smem<C>(p->S, nst);
     auto kern = k_sweep_tma<C>;
-    KORE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    KORE_TRY(kore_allow_max_dyn_smem(kern, p->device));
     int occ = 0;
     KORE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTmaThreads, smem));
     if (occ < 1) return KORE_EINVAL;

@@ -165,6 +165,32 @@ def kernel_launches():
     return int(L.load().kore_kernel_launches())
 
 
+def forced_sweep(pencil, omegas, b, precision="mixed", group=16, refine_tol=0.0, scale=1.0):
+    """Forced solves over a frequency sweep on one eigen pencil.
+
+    kore's forced matrix at forcing frequency w is ||B||_F (A_eig - i w B_eig)
+    (``bin/assemble.py:582-584``), so each forced solve of ``bin/solve.py:207-268`` is the
+    shifted solve x_w = (A_eig - i w B_eig)^-1 b_w / scale with scale = ||B||_F.  The
+    frequencies are factorised and solved ``group`` at a time in batched kernels.
+
+    b: (n,) right-hand side shared by every frequency, or (n, F) one per frequency.
+    Returns (X (n, F), per-group wall seconds).
+    """
+    om = np.asarray(omegas, dtype=np.float64).ravel()
+    F = len(om)
+    b = np.asarray(b)
+    X = np.empty((pencil.n, F), dtype=np.complex128)
+    times = []
+    for g0 in range(0, F, group):
+        sl = slice(g0, min(F, g0 + group))
+        t = time.perf_counter()
+        pencil.factor_shifts(1j * om[sl], precision)
+        rhs = (b[:, sl] if b.ndim == 2 else np.repeat(b.reshape(-1, 1), sl.stop - sl.start, axis=1)) / scale
+        X[:, sl] = pencil.solve(rhs, refine_tol=refine_tol)
+        times.append(time.perf_counter() - t)
+    return X, times
+
+
 class EPS:
     """Shift-and-invert Krylov-Schur eigensolver with the slepc4py EPS call sequence
     that ``bin/solve.py:91-123`` uses."""

@@ -46,3 +46,17 @@ def test_multiplication_operator_lambda0_is_chebyshev_product():
 def test_ncheb_rule():
     # bin/parameters.py:6-16
     assert ncheb(1e-3) == 68 and ncheb(1e-7) == 428 and ncheb(0) == 48
+
+
+def test_forced_matrix_is_scaled_shift_of_eigen_pencil():
+    """kore's forced matrix at frequency w equals ||B||_F (A_eig - i w B_eig), and the
+    forcing column built alone equals the one assembled with the forced matrix; the
+    batched frequency sweep relies on both."""
+    from kore_gb300.assembly import forcing_vector, hydro_pencil
+    m, symm, Ek, N, lmax, ricb = 2, 1, 1e-4, 24, 13, 0.35
+    Ae, Be, nrm = hydro_pencil(m, symm, Ek, N, lmax, ricb, with_norm=True)
+    for w in (-1.3, 0.0, 0.7):
+        Af, bf = hydro_pencil(m, symm, Ek, N, lmax, ricb, forcing=10, forcing_frequency=w)
+        M = nrm * (Ae - (1j * w) * Be)
+        assert abs(Af - M).max() <= 1e-12 * abs(Af).max()
+        assert abs(bf - forcing_vector(m, symm, N, lmax, ricb, 10, w)).max() == 0
