@@ -36,6 +36,8 @@ extern "C" {
 #define KORE_ETIMEOUT    6   /* a bounded device wait ran out (error flag set by a kernel) */
 #define KORE_ENOTFACTORED 7  /* solve/eigs before kore_factor */
 #define KORE_ENAN        8   /* NaN or Inf in a solution (bin/solve.py:263-268) */
+#define KORE_EPENDING    9   /* kore_batch_poll: the request has not finished yet */
+#define KORE_ECANCELLED 10   /* kore_batch_destroy dropped the request before it started */
 
 /* factorisation precisions */
 #define KORE_PREC_FP64   0   /* complex128 block LU, complex128 sweeps */
@@ -189,6 +191,73 @@ int kore_profile(kore_plan *plan, int enable, double *out);
 
 /* Device bytes held by the plan (CSR copies + factors + Krylov workspace). */
 int kore_plan_bytes(const kore_plan *plan, int64_t *bytes);
+
+/*
+ * Upper bound of the device bytes a plan of this pencil holds once it has factorised
+ * nshift shifts in `precision` and, for ncv > 0, run an eigensolve with ncv basis
+ * vectors: the plan's copies of A and B, the factors and the solve and Krylov
+ * workspaces.  Computed from the sizes alone (nothing is allocated); the serving
+ * queue below admits requests by it.
+ */
+int kore_plan_estimate_bytes(const kore_pencil_desc *desc, int precision, int nshift, int ncv, int64_t *bytes);
+
+/*
+ * Serving: a queue of eigen and forced solves of different pencils run by `workers`
+ * host threads, each on its own plan and CUDA stream, admitted by device memory.
+ * There is no counterpart in the reference, which runs one bin/solve.py process per
+ * problem; a request does what one such run does (eigen: kore_eigs at its target;
+ * forced: kore_solve at its shift) and writes the same results.
+ *
+ *  - Admission: a request starts when the estimate of its plan (kore_plan_estimate_bytes)
+ *    fits in hbm_budget next to the plans in use and cached; idle cached plans are
+ *    freed oldest first to make room.  Requests start in arrival order, except that one
+ *    which does not fit yet does not hold back later ones that do (until it has waited
+ *    longer than 200 ms, after which nothing new starts before it).
+ *  - Factor cache: requests with the same non-zero pencil_key share uploaded plans; a
+ *    request whose (key, shift, precision) matches an idle cached plan skips the
+ *    upload and the factorisation.  pencil_key = 0: the plan is freed after the request.
+ *  - The caller keeps the pencil arrays, the right-hand side and the output buffers
+ *    alive until kore_batch_poll reports the request finished.
+ *  - A result does not depend on what else is running: each request runs on its own
+ *    plan, and every kernel reduces in a fixed order.
+ */
+#define KORE_REQ_EIGEN  0
+#define KORE_REQ_FORCED 1
+
+typedef struct kore_batch kore_batch;
+
+typedef struct {
+    int32_t kind;                     /* KORE_REQ_EIGEN or KORE_REQ_FORCED */
+    const kore_pencil_desc *pencil;   /* read when the request starts */
+    uint64_t pencil_key;              /* caller's name for the pencil (0: no sharing) */
+    int32_t precision;                /* KORE_PREC_* */
+    double sigma_re, sigma_im;        /* forced: the shift; eigen: the target (opts.target_*) */
+    kore_eps_opts opts;               /* eigen */
+    const double *rhs;                /* forced: n complex right-hand side */
+    double rhs_scale;                 /* forced: solves with rhs / rhs_scale (0 means 1) */
+    double refine_tol;                /* forced, mixed precision (<= 0: 1e-14) */
+    double *x;                        /* forced: n complex solution */
+    double *evals;                    /* eigen: 2 * max_pairs doubles */
+    double *evecs;                    /* eigen: NULL or 2 * n * max_pairs doubles */
+    int32_t max_pairs;
+    int32_t *nconv;                   /* eigen: converged pairs */
+    double *timing_ms;                /* NULL or 3 doubles: queued, running, submit to finish */
+} kore_request;
+
+/* hbm_budget <= 0: 90% of the device's free memory at creation. */
+int kore_batch_create(int device, int64_t hbm_budget, int workers, kore_batch **batch);
+/* Copies *req (not the arrays it points to) and returns a ticket. */
+int kore_batch_submit(kore_batch *batch, const kore_request *req, uint64_t *ticket);
+/*
+ * KORE_OK when the request has finished (*status = its status; the ticket is then
+ * released), KORE_EPENDING when it has not after wait_ms milliseconds (-1: wait).
+ */
+int kore_batch_poll(kore_batch *batch, uint64_t ticket, int wait_ms, int *status);
+/* out[8]: submitted, finished, running, queued, device bytes in plans, factor-cache
+ * hits, plans created, plans freed to make room */
+int kore_batch_stats(kore_batch *batch, int64_t *out);
+/* Waits for running requests, cancels queued ones (KORE_ECANCELLED), frees all plans. */
+int kore_batch_destroy(kore_batch *batch);
 
 /* Number of kernels this library launched since load (for launch accounting). */
 int64_t kore_kernel_launches(void);

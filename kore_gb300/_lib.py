@@ -14,14 +14,19 @@ LIB_PATH = os.path.join(_HERE, "libkoregpu.so")
 KORE_OK = 0
 STATUS = {
     0: "KORE_OK", 1: "KORE_EINVAL", 2: "KORE_ENOMEM", 3: "KORE_ECUDA", 4: "KORE_ESINGULAR",
-    5: "KORE_ENOCONV", 6: "KORE_ETIMEOUT", 7: "KORE_ENOTFACTORED", 8: "KORE_ENAN",
+    5: "KORE_ENOCONV", 6: "KORE_ETIMEOUT", 7: "KORE_ENOTFACTORED", 8: "KORE_ENAN", 9: "KORE_EPENDING",
+    10: "KORE_ECANCELLED",
 }
+KORE_EPENDING = 9
+REQ_EIGEN, REQ_FORCED = 0, 1
 PREC = {"fp64": 0, "mixed": 1}
 WHICH = {"LM": 0, "SM": 1, "LR": 2, "SR": 3, "LI": 4, "SI": 5, "TM": 6, "TR": 7, "TI": 8}
 
 # every function include/kore_gpu.h declares
-EXPORTS = ("kore_plan_create", "kore_factor", "kore_factor_shifts", "kore_solve", "kore_solve_dev", "kore_solve_dev_noalloc", "kore_eigs",
-           "kore_residual", "kore_plan_stream", "kore_profile", "kore_plan_bytes", "kore_kernel_launches",
+EXPORTS = ("kore_plan_create", "kore_factor", "kore_factor_shifts", "kore_solve", "kore_solve_dev",
+           "kore_solve_dev_noalloc", "kore_eigs", "kore_residual", "kore_plan_stream", "kore_profile",
+           "kore_plan_bytes", "kore_plan_estimate_bytes", "kore_batch_create", "kore_batch_submit",
+           "kore_batch_poll", "kore_batch_stats", "kore_batch_destroy", "kore_kernel_launches",
            "kore_status_string", "kore_plan_destroy")
 
 
@@ -83,6 +88,27 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Request(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("pencil", C.POINTER(PencilDesc)),
+        ("pencil_key", C.c_uint64),
+        ("precision", C.c_int32),
+        ("sigma_re", C.c_double),
+        ("sigma_im", C.c_double),
+        ("opts", EpsOpts),
+        ("rhs", C.c_void_p),
+        ("rhs_scale", C.c_double),
+        ("refine_tol", C.c_double),
+        ("x", C.c_void_p),
+        ("evals", C.c_void_p),
+        ("evecs", C.c_void_p),
+        ("max_pairs", C.c_int32),
+        ("nconv", C.POINTER(C.c_int32)),
+        ("timing_ms", C.c_void_p),
+    ]
+
+
 _lib = None
 _load_error = None
 
@@ -105,6 +131,12 @@ def _bind(lib):
     lib.kore_status_string.argtypes = [C.c_int]
     lib.kore_status_string.restype = C.c_char_p
     lib.kore_plan_destroy.argtypes = [P]
+    lib.kore_plan_estimate_bytes.argtypes = [C.POINTER(PencilDesc), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64)]
+    lib.kore_batch_create.argtypes = [C.c_int, C.c_int64, C.c_int, C.POINTER(P)]
+    lib.kore_batch_submit.argtypes = [P, C.POINTER(Request), C.POINTER(C.c_uint64)]
+    lib.kore_batch_poll.argtypes = [P, C.c_uint64, C.c_int, C.POINTER(C.c_int)]
+    lib.kore_batch_stats.argtypes = [P, P]
+    lib.kore_batch_destroy.argtypes = [P]
     for name in EXPORTS:
         if name not in ("kore_kernel_launches", "kore_status_string"):
             getattr(lib, name).restype = C.c_int

@@ -473,6 +473,47 @@ int kore_plan_bytes(const kore_plan *p, int64_t *bytes) {
 
 int64_t kore_kernel_launches(void) { return g_kore_launches.load(); }
 
+int kore_plan_estimate_bytes(const kore_pencil_desc *d, int precision, int nshift, int ncv, int64_t *bytes) {
+    if (!d || !bytes || d->n <= 0 || d->nblocks <= 0 || !d->block_sizes || !d->a_indptr || nshift <= 0) return KORE_EINVAL;
+    if (precision != KORE_PREC_FP64 && precision != KORE_PREC_MIXED) return KORE_EINVAL;
+    // the sizes the plan and ensure_factor_storage allocate (see create() and factor.cu)
+    const int64_t K = d->nblocks;
+    int64_t S = 0;
+    for (int64_t i = 0; i < K; ++i) S = std::max<int64_t>(S, d->block_sizes[i]);
+    S = (S + 3) & ~3LL;
+    const int64_t np = K * S, SS = S * S, na = d->a_nnz, nb = d->b_nnz;
+    std::vector<int64_t> Ks;
+    for (int64_t Kl = K; Kl > 1; Kl -= Kl / 2) Ks.push_back(Kl);
+    const int64_t nlev = (int64_t)Ks.size();
+    int64_t lu = 0, nodd_max = 1;
+    for (int64_t l = 0; l < nlev; ++l) {
+        if (l > 0) lu += 2 * Ks[l];
+        nodd_max = std::max<int64_t>(nodd_max, Ks[l] / 2);
+    }
+    lu = std::max<int64_t>(lu, 1);
+    int64_t maxrow = 1;
+    for (int64_t r = 0; r < d->n; ++r) maxrow = std::max<int64_t>(maxrow, d->a_indptr[r + 1] - d->a_indptr[r]);
+    const int64_t ne = nlev > 0 ? Ks[0] - Ks[0] / 2 : 0, nt = (S + 31) / 32;
+    const int64_t ell = std::max<int64_t>(ne * nt * 32 * ((maxrow + 7) & ~7LL), 1);
+    const int64_t e = (precision == KORE_PREC_FP64) ? 16 : 8, c = nshift;
+    int64_t b = 0;
+    // plan: A (CSR, split rows, padded level-0 rows), B, permutation, vectors
+    b += (np + 1) * 4 + na * 20 + 2 * np * 4;
+    b += (2 * np + 1) * 4 + 2 * na * 12;
+    b += 2 * ell * 4 + np * 4;
+    b += (np + 1) * 4 + nb * 12;
+    b += np * 8 + K * 4 + nlev * (int64_t)sizeof(BcrLevel) + 6 * np * 16 + 8192 * 8 + 1024;
+    // factors and solve workspace of c shifts
+    b += c * (4 * K * SS * e + lu * SS * e + nodd_max * 4 * SS * e + 3 * np * e + np * 8 + 3 * nodd_max * S * 4);
+    b += c * (3 * np * 16 + 2 * (np / 64 + np / 8 + 1024) * 8 + (3 * nlev + 1) * K * 4 + ell * e + 128);
+    b += 2 * d->n * c * 16;   // kore_solve's device copies of b and x
+    // Krylov basis, its copy and the projected-problem workspace
+    if (ncv > 0) b += 2 * np * (int64_t)(ncv + 1) * 16 + (int64_t)(65 * 64 * 4 + 8 * 65 + 2048 * 65 + 4096) * 16;
+    b += 128LL << 20;   // allocation granularity of ~50 buffers
+    *bytes = b;
+    return KORE_OK;
+}
+
 const char *kore_status_string(int s) {
     switch (s) {
         case KORE_OK: return "ok";
@@ -484,6 +525,8 @@ const char *kore_status_string(int s) {
         case KORE_ETIMEOUT: return "a bounded device wait ran out";
         case KORE_ENOTFACTORED: return "plan not factorised";
         case KORE_ENAN: return "NaN or Inf in the solution";
+        case KORE_EPENDING: return "the request has not finished";
+        case KORE_ECANCELLED: return "the request was cancelled before it started";
     }
     return "unknown status";
 }

@@ -30,15 +30,11 @@ def _csr(M, dtype):
     return (L.as_i32(M.indptr), L.as_i32(M.indices), np.ascontiguousarray(M.data, dtype=dtype))
 
 
-class Pencil:
-    """A (complex128) and optionally B (float64) on the device in l-major block form.
+class PencilData:
+    """The host CSR arrays of A (complex128) and B (float64, optional) with the l-major
+    layout, held in the form ``kore_pencil_desc`` points to (``desc``)."""
 
-    ``layout`` is a :class:`~kore_gb300.structure.Layout` (or the kore parameters to
-    derive one from).  The device copies are owned by the plan; ``close()`` frees them.
-    """
-
-    def __init__(self, A, B=None, layout=None, params=None, device=0):
-        self.lib = L.load()
+    def __init__(self, A, B=None, layout=None, params=None):
         if layout is None:
             if params is None:
                 raise ValueError("need a layout or the kore parameters")
@@ -66,9 +62,32 @@ class Pencil:
         d.perm = self._perm.ctypes.data_as(C.POINTER(C.c_int64))
         d.nblocks = len(self._bs)
         d.block_sizes = self._bs.ctypes.data_as(C.POINTER(C.c_int32))
+        self.desc = d
+
+    def estimate_bytes(self, precision="mixed", nshift=1, ncv=0):
+        """Upper bound of the device bytes of a plan of this pencil (kore_plan_estimate_bytes)."""
+        out = C.c_int64()
+        L.check(L.load().kore_plan_estimate_bytes(C.byref(self.desc), L.PREC[precision], int(nshift), int(ncv),
+                                                   C.byref(out)), "kore_plan_estimate_bytes")
+        return int(out.value)
+
+
+class Pencil:
+    """A (complex128) and optionally B (float64) on the device in l-major block form.
+
+    ``layout`` is a :class:`~kore_gb300.structure.Layout` (or the kore parameters to
+    derive one from).  The device copies are owned by the plan; ``close()`` frees them.
+    """
+
+    def __init__(self, A, B=None, layout=None, params=None, device=0):
+        self.lib = L.load()
+        self.data = PencilData(A, B, layout, params)
+        self.layout = self.data.layout
+        self.n = self.data.n
         self._plan = C.c_void_p()
         t = time.perf_counter()
-        L.check(self.lib.kore_plan_create(C.byref(d), int(device), C.byref(self._plan)), "kore_plan_create")
+        L.check(self.lib.kore_plan_create(C.byref(self.data.desc), int(device), C.byref(self._plan)),
+                "kore_plan_create")
         self.create_s = time.perf_counter() - t
         self.sigma = None
         self.precision = None

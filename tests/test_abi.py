@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
 def test_status_strings_and_counter():
     from kore_gb300 import _lib
     lib = _lib.load()
-    for code in range(9):
+    for code in range(11):
         assert lib.kore_status_string(code)
     assert lib.kore_kernel_launches() >= 0
 
@@ -45,3 +45,33 @@ def test_plan_create_rejects_bad_desc():
     plan = ctypes.c_void_p()
     assert lib.kore_plan_create(ctypes.byref(d), 0, ctypes.byref(plan)) == 1
     assert lib.kore_plan_create(None, 0, ctypes.byref(plan)) == 1
+
+
+def test_estimate_bytes_bounds_the_allocations():
+    """kore_plan_estimate_bytes (host arithmetic only) is at least the factor and
+    workspace sizes of the block structure and grows with precision, shifts and ncv."""
+    import numpy as np
+    from conftest import load_case
+    from kore_gb300.solver import PencilData
+    from kore_gb300.structure import layout_from_params
+    meta, A, B = load_case("shell_m2_ek1e-4")
+    P = PencilData(A, B, layout=layout_from_params(meta))
+    K = len(P.layout.block_sizes)
+    S = (int(P.layout.block_sizes.max()) + 3) // 4 * 4
+    e64, e32 = P.estimate_bytes("fp64"), P.estimate_bytes("mixed")
+    assert e64 > e32 >= 4 * K * S * S * 8
+    assert P.estimate_bytes("mixed", nshift=4) > 3 * (e32 - (128 << 20))
+    assert P.estimate_bytes("mixed", ncv=32) >= e32 + 2 * K * S * 33 * 16
+
+
+def test_batch_api_rejects_bad_arguments():
+    """The serving entry points validate their arguments before starting anything."""
+    from kore_gb300 import _lib
+    lib = _lib.load()
+    b = ctypes.c_void_p()
+    assert lib.kore_batch_create(0, 0, 0, ctypes.byref(b)) == 1          # no workers
+    t = ctypes.c_uint64()
+    assert lib.kore_batch_submit(None, None, ctypes.byref(t)) == 1
+    st = ctypes.c_int()
+    assert lib.kore_batch_poll(None, 1, 0, ctypes.byref(st)) == 1
+    assert lib.kore_batch_destroy(None) == 0
