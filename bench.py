@@ -338,13 +338,112 @@ def forced_bench(args, local):
     print(json.dumps(line), flush=True)
 
 
+# Serving: a seeded Poisson stream of requests over a pool of pencils drawn from the
+# serving ranges (lmax in [60, 600], N in [48, 400], Ek log-uniform in [1e-7, 1e-4],
+# m in 0..8); 70% eigen (nev 4..16, target i*U[-2, 2]) and 30% forced (forcing 10,
+# shift i*U[-2, 2]), at each arrival rate in `rates` (requests/s).
+SERVE = {
+    "serve5": dict(pool=8, requests=120, rates=(2.0, 6.0), workers=4),
+    "serve5s": dict(pool=3, requests=24, rates=(4.0,), workers=3, small=True),
+}
+
+
+def serve_pool(count, seed=11, small=False):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        m = int(rng.integers(0, 9))
+        N = 2 * int(rng.integers(24, 201)) if not small else 2 * int(rng.integers(12, 33))
+        lmax = int(rng.integers(60, 601)) if not small else int(rng.integers(20, 61))
+        if (lmax - m + 1) % 2:
+            lmax += 1
+        out.append(dict(m=m, N=N, lmax=lmax, Ek=float(10 ** rng.uniform(-7, -4)), ricb=0.35))
+    return out
+
+
+def serve_bench(args, local):
+    """Serving queue (kore_gb300.serve.Server): p50/p99 request latency and throughput of
+    a Poisson request stream at several arrival rates."""
+    import torch
+    from kore_gb300 import build as kb
+    from kore_gb300.assembly import forcing_vector, hydro_params, hydro_pencil
+    from kore_gb300.serve import PencilData, Server
+    from kore_gb300.structure import layout_from_params
+    kb.build()
+    torch.cuda.set_device(local)
+    c = SERVE[args.workload]
+    pool = []
+    for d in serve_pool(c["pool"], small=c.get("small", False)):
+        A, B, nrm = hydro_pencil(d["m"], 1, d["Ek"], d["N"], d["lmax"], d["ricb"], with_norm=True)
+        b = (forcing_vector(d["m"], 1, d["N"], d["lmax"], d["ricb"], 10).toarray().ravel() / nrm
+             if d["m"] >= 1 else None)
+        P = PencilData(A, B, layout=layout_from_params(hydro_params(d["m"], 1, d["Ek"], d["N"], d["lmax"],
+                                                                    d["ricb"])))
+        pool.append((d, P, b))
+    rng = np.random.default_rng(21)
+    per_rate = []
+    for rate in c["rates"]:
+        reqs = []
+        t = 0.0
+        for _ in range(c["requests"]):
+            t += rng.exponential(1.0 / rate)
+            i = int(rng.integers(len(pool)))
+            d, P, b = pool[i]
+            eigen = rng.uniform() < 0.7 or b is None
+            reqs.append((t, i, eigen, int(rng.integers(4, 17)), 1j * float(rng.uniform(-2, 2))))
+        with Server(device=local, workers=c["workers"]) as srv:
+            # warm-up: one request per pencil
+            for d, P, b in pool:
+                srv.result(srv.submit_eigen(P, 0.5j, 4, seed=1))
+            tickets = []
+            t0 = time.perf_counter()
+            for (ta, i, eigen, nev, tgt) in reqs:
+                now = time.perf_counter() - t0
+                if ta > now:
+                    time.sleep(ta - now)
+                d, P, b = pool[i]
+                if eigen:
+                    tickets.append((srv.submit_eigen(P, tgt, nev, seed=len(tickets) + 1), nev, True))
+                else:
+                    tickets.append((srv.submit_forced(P, tgt, b), 0, False))
+            lat, ok, short = [], 0, 0
+            for tk, nev, eigen in tickets:
+                r = srv.poll(tk, wait_ms=-1)
+                lat.append(r["total_ms"])
+                if r["status"] == 0:
+                    ok += 1
+                    if eigen and r["nconv"] < nev:
+                        short += 1
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+        per_rate.append({"arrival_rate": rate, "requests": len(reqs), "ok": ok, "eigen_short_of_nev": short,
+                         "throughput": len(reqs) / wall, "p50_ms": float(np.percentile(lat, 50)),
+                         "p99_ms": float(np.percentile(lat, 99)), "factor_cache_hits": st["factor_cache_hits"],
+                         "plans_created": st["plans_created"], "plans_evicted": st["plans_evicted"]})
+    best = max(per_rate, key=lambda r: r["throughput"])
+    line = {
+        "metric": "served solves/s and p50/p99 latency (Poisson stream, 70% eigen / 30% forced, mixed precision)",
+        "value": best["throughput"], "unit": "requests/s", "n_gpus": 1, "steps": sum(r["requests"] for r in per_rate),
+        "warmup": len(pool), "ms_per_step": best["p50_ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 factor + f64 refinement/Krylov",
+        "data": "synthetic: pencils assembled from the kore parameters",
+        "config": {"workload": f"serving: {c['pool']} pencils "
+                               + ", ".join(f"(m={d['m']}, N={d['N']}, lmax={d['lmax']}, Ek={d['Ek']:.2g})"
+                                           for d, _, _ in pool)
+                               + f"; {c['requests']} requests per arrival rate; {c['workers']} workers",
+                   "parallelism": "replicas x1"},
+        "rates": per_rate,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="shell2", choices=sorted(WORKLOADS) + sorted(FORCED))
+    ap.add_argument("--workload", default="shell2", choices=sorted(WORKLOADS) + sorted(FORCED) + sorted(SERVE))
     ap.add_argument("--fp64-steps", type=int, default=None)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -359,6 +458,10 @@ def main():
     if args.workload in FORCED:
         if rank == 0:
             forced_bench(args, local)
+        return
+    if args.workload in SERVE:
+        if rank == 0:
+            serve_bench(args, local)
         return
 
     import torch
