@@ -259,6 +259,15 @@ int kore_batch_stats(kore_batch *batch, int64_t *out);
 /* Waits for running requests, cancels queued ones (KORE_ECANCELLED), frees all plans. */
 int kore_batch_destroy(kore_batch *batch);
 
+/*
+ * Self-test of the tensor-core complex64 GEMM that the mixed-precision factorisation
+ * uses (tcgen05, 3xTF32): nmat seeded S x S products, one and two per job, with and
+ * without accumulation into C, checked against an FP64 product on the device.
+ * *max_rel_err = max over entries of |C - C_fp64| / sum_k |a_ik| |b_kj|.
+ * No counterpart in the reference; a diagnostic for the kernel.
+ */
+int kore_tc_selftest(int device, int S, int nmat, double *max_rel_err);
+
 /* Number of kernels this library launched since load (for launch accounting). */
 int64_t kore_kernel_launches(void);
 

@@ -571,7 +571,11 @@ int factor_levels(kore_plan *p) {
             const int th = std::min(1024, ((S + 31) / 32) * 32);
             k_even_l0<C><<<g, th, 0, st>>>(v, lv);
             KORE_LAUNCHED(1);
+        } else if (sizeof(C) == sizeof(float2)) {
+            // complex64: tensor cores (3xTF32)
+            KORE_TRY(kore_even_update_tc(p, lv));
         } else {
+            // complex128: FP64 CUDA cores
             const int jobs = 3 * lv.neven * ns;
             for (int j0 = 0; j0 < jobs; j0 += 65535) {
                 dim3 g(kore_div_up(S, kGT), kore_div_up(S, kGT), std::min(65535, jobs - j0));
@@ -647,7 +651,7 @@ int ensure_factor_storage(kore_plan *p, int cap, size_t elt) {
                      (void **)&p->d_rscale, (void **)&p->d_piv, (void **)&p->d_pidx, (void **)&p->d_used,
                      (void **)&p->d_sigma, (void **)&p->d_minf, (void **)&p->d_bb, (void **)&p->d_xb, (void **)&p->d_rb,
                      (void **)&p->d_bn, (void **)&p->d_rn, (void **)&p->d_part, (void **)&p->d_ir,
-                     (void **)&p->d_cnt, &p->d_ell_val};
+                     (void **)&p->d_cnt, &p->d_ell_val, &p->d_tcplanes, &p->d_tctab};
     for (void **b : bufs) {
         if (*b) cudaFree(*b);
         *b = nullptr;
@@ -683,6 +687,12 @@ int ensure_factor_storage(kore_plan *p, int cap, size_t elt) {
     KORE_TRY(kore_alloc(p, (void **)&p->d_ir, c * sizeof(IrState)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_cnt, c * (size_t)(3 * p->nlev + 1) * p->K * sizeof(int)));
     KORE_TRY(kore_alloc(p, &p->d_ell_val, c * std::max<int64_t>(p->ell_stride(), 1) * elt));
+    if (elt == sizeof(float2)) {
+        int64_t pl = 0, tb = 0;
+        kore_tc_level_bytes(p, cap, &pl, &tb);
+        KORE_TRY(kore_alloc(p, &p->d_tcplanes, (size_t)pl));
+        KORE_TRY(kore_alloc(p, &p->d_tctab, (size_t)tb));
+    }
     KORE_CUDA_TRY(cudaMemset(p->d_LU, 0, c * p->lu_stride() * elt));
     KORE_CUDA_TRY(cudaMemset(p->d_piv, 0, c * p->p_stride() * sizeof(int)));
     KORE_CUDA_TRY(cudaMemset(p->d_pidx, 0xff, c * p->p_stride() * sizeof(int)));

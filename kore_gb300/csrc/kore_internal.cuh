@@ -104,6 +104,10 @@ struct kore_plan {
     int *d_ell_col = nullptr;         // padded slot of the coupled unknown, -1 for padding
     int *d_ell_src = nullptr;         // entry of A in the permuted CSR, -1 for padding
     void *d_ell_val = nullptr;        // per shift: rscale_row * A entry, factor precision
+    // complex64 factorisation: TF32 split planes and job table of the tensor-core
+    // even-block updates (gemm_tc.cu), sized for the largest level
+    void *d_tcplanes = nullptr;
+    void *d_tctab = nullptr;
 
     int64_t f_stride() const { return (int64_t)K * S * S; }
     int64_t lu_stride() const { return lu_mats * (int64_t)S * S; }
@@ -161,6 +165,10 @@ int kore_alloc(kore_plan *p, void **ptr, size_t bytes);
 void kore_build_levels(kore_plan *p);
 // factorise A - sigma_s B for nshift shifts (interleaved re, im) at once
 int kore_factor_impl(kore_plan *p, int nshift, const double *sigmas, int precision);
+
+// gemm_tc.cu: tensor-core (tcgen05, 3xTF32) even-block update of a level >= 1, complex64
+int kore_even_update_tc(kore_plan *p, const BcrLevel &lv);
+void kore_tc_level_bytes(const kore_plan *p, int cap, int64_t *plane_bytes, int64_t *table_bytes);
 
 // sweep.cu
 // x_s = (A - sigma_s B)^-1 b_s for every factorised shift s on padded l-major

@@ -63,6 +63,15 @@ __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, u
         : "memory");
 }
 
+// 3-D tiled tensor copy global -> shared, completing on `bar`.
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1, int c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
 __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap *map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
@@ -83,3 +92,8 @@ __device__ __forceinline__ void named_sync(int id, int nthreads) {
 // block's rows or columns return zeros.  real_bytes is 4 (complex64) or 8 (complex128).
 int kore_encode_block_map(CUtensorMap *map, const void *base, int real_bytes, int S, int64_t nblk, int nshift,
                           int64_t shift_stride, int box_rows, int box_cols);
+
+// 3-D float32 tensor map (dims innermost first, strides in bytes of dims 1 and 2) with
+// an optional 128-byte swizzle (box[0] * 4 must then be 128 or less).
+int kore_encode_f32_3d(CUtensorMap *map, const void *base, const uint64_t dims[3], const uint64_t strides[2],
+                       const uint32_t box[3], int swizzle128);
