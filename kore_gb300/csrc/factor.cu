@@ -54,6 +54,7 @@ struct FV {
     double *rscale;
     C *Dinv, *G, *H, *Dw, *LU, *T;
     int *piv, *pidx, *used, *err;
+    const int *cc_ptr, *cc_row, *cc_src;
     int64_t f_stride, lu_stride, t_stride, p_stride;
 };
 
@@ -67,6 +68,7 @@ FV<C> make_fv(kore_plan *p) {
     v.Dinv = static_cast<C *>(p->d_Dinv); v.G = static_cast<C *>(p->d_Gm); v.H = static_cast<C *>(p->d_Hm);
     v.Dw = static_cast<C *>(p->d_Dw); v.LU = static_cast<C *>(p->d_LU); v.T = static_cast<C *>(p->d_T);
     v.piv = p->d_piv; v.pidx = p->d_pidx; v.used = p->d_used; v.err = p->d_err;
+    v.cc_ptr = p->d_cc_ptr; v.cc_row = p->d_cc_row; v.cc_src = p->d_cc_src;
     v.f_stride = p->f_stride(); v.lu_stride = p->lu_stride(); v.t_stride = p->t_stride(); v.p_stride = p->p_stride();
     return v;
 }
@@ -175,13 +177,12 @@ __global__ void k_Dw_scatter(FV<C> v, int nshift) {
     }
 }
 
-// T_o = [Dw_j | L | U | I] for the odd blocks j of level lv, all shifts; L, U copied
-// from the dense couplings (levels >= 1) or zeroed (level 0: scattered from the CSR
-// next).  stride 0 selects block 0 (the top of the reduction).
+// T_o = [Dw_j | I] for the odd blocks j of level lv, all shifts.  stride 0 selects
+// block 0 (the top of the reduction).
 template <typename C>
 __global__ void k_T_fill(FV<C> v, BcrLevel lv, int nodd, int nshift) {
     const int S = v.S;
-    const int64_t SS = (int64_t)S * S, per = 4 * SS, pershift = (int64_t)nodd * per, total = pershift * nshift;
+    const int64_t SS = (int64_t)S * S, per = 2 * SS, pershift = (int64_t)nodd * per, total = pershift * nshift;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int64_t s = idx / pershift;
@@ -194,34 +195,11 @@ __global__ void k_T_fill(FV<C> v, BcrLevel lv, int nodd, int nshift) {
         const int64_t j = q * lv.stride;           // original block
         C val;
         if (part == 0) val = v.Dw[s * v.f_stride + j * SS + w];
-        else if (part == 3) {
+        else {
             const int c = (int)(w / S), r = (int)(w - (int64_t)c * S);
             val = (r == c) ? cone<C>() : czero<C>();
-        } else if (lv.lu_L < 0) val = czero<C>();
-        else val = v.LU[s * v.lu_stride + ((part == 1 ? lv.lu_L : lv.lu_U) + q) * SS + w];
+        }
         v.T[s * v.t_stride + o * per + e] = val;
-    }
-}
-
-// Level 0: one warp per (shift, row of an odd block j): scatter rs * L_j and rs * U_j into T_o.
-template <typename C>
-__global__ void k_T_scatter_LU(FV<C> v, int nodd, int nshift) {
-    const int lane = threadIdx.x & 31;
-    const int S = v.S;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t SS = (int64_t)S * S, rows = (int64_t)nodd * S;
-    for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < rows * nshift; w += nw) {
-        const int64_t s = w / rows, wr = w - s * rows;
-        const int64_t o = wr / S;
-        const int r = (int)(wr - o * S);
-        const int64_t j = 2 * o + 1;
-        const int64_t p = j * S + r;
-        const double rs = v.rscale[s * v.np + p];
-        C *To = v.T + s * v.t_stride + o * 4 * SS;
-        for (int e = v.arow[p] + lane; e < v.asplit[2 * p]; e += 32)
-            To[r + (int64_t)(S + v.acol[e] - (j - 1) * S) * S] = from_c128<C>(rs * v.aval[e]);
-        for (int e = v.asplit[2 * p + 1] + lane; e < v.arow[p + 1]; e += 32)
-            To[r + (int64_t)(2 * S + v.acol[e] - (j + 1) * S) * S] = from_c128<C>(rs * v.aval[e]);
     }
 }
 
@@ -240,7 +218,7 @@ __global__ void __launch_bounds__(1024) k_panel(FV<C> v, int k0) {
     __shared__ C s_dinv;
     __shared__ int s_piv[NB];
     const int64_t o = blockIdx.x, sh = blockIdx.y;
-    C *T = v.T + sh * v.t_stride + o * 4 * (int64_t)S * S;
+    C *T = v.T + sh * v.t_stride + o * 2 * (int64_t)S * S;
     int *piv = v.piv + sh * v.p_stride + o * S, *pidx = v.pidx + sh * v.p_stride + o * S;
     int *used = v.used + sh * v.p_stride + o * S;
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -321,7 +299,7 @@ __global__ void __launch_bounds__(256) k_update(FV<C> v, int k0, int nb, int col
     __shared__ C tp[TW][NB];
     const int S = v.S;
     const int64_t o = blockIdx.y, sh = blockIdx.z;
-    C *T = v.T + sh * v.t_stride + o * 4 * (int64_t)S * S;
+    C *T = v.T + sh * v.t_stride + o * 2 * (int64_t)S * S;
     const int *piv = v.piv + sh * v.p_stride + o * S, *pidx = v.pidx + sh * v.p_stride + o * S;
     const int j0 = col_begin + blockIdx.x * TW;
     const int tw = min(TW, col_end - j0);
@@ -346,8 +324,7 @@ __global__ void __launch_bounds__(256) k_update(FV<C> v, int k0, int nb, int col
     }
 }
 
-// Solution rows by pivot: Dinv_j[k,:] = T[piv[k], 3S:4S), G_j from T[:, S:2S),
-// H_j from T[:, 2S:3S)  (column-major S x S outputs), all shifts.
+// Solution rows by pivot: Dinv_j[k,:] = T[piv[k], S:2S)  (column-major S x S), all shifts.
 template <typename C>
 __global__ void k_extract(FV<C> v, BcrLevel lv, int nodd, int top, int nshift) {
     const int S = v.S;
@@ -359,15 +336,10 @@ __global__ void k_extract(FV<C> v, BcrLevel lv, int nodd, int top, int nshift) {
         const int64_t o = ws / SS;
         const int64_t w = ws - o * SS;
         const int c = (int)(w / S), k = (int)(w - (int64_t)c * S);
-        const C *T = v.T + sh * v.t_stride + o * 4 * SS;
+        const C *T = v.T + sh * v.t_stride + o * 2 * SS;
         const int p = v.piv[sh * v.p_stride + o * S + k];
         const int64_t j = top ? 0 : (2 * o + 1) * lv.stride;
-        const int64_t out = sh * v.f_stride + j * SS + w;
-        v.Dinv[out] = T[p + (int64_t)(3 * S + c) * S];
-        if (!top) {
-            v.G[out] = T[p + (int64_t)(S + c) * S];
-            v.H[out] = T[p + (int64_t)(2 * S + c) * S];
-        }
+        v.Dinv[sh * v.f_stride + j * SS + w] = T[p + (int64_t)(S + c) * S];
     }
 }
 
@@ -417,47 +389,17 @@ __global__ void k_even_l0(FV<C> v, BcrLevel lv) {
     }
 }
 
-// Batched dense update of the even blocks at levels >= 1, one GEMM job per
-// (shift, even block, kind): kind 0: Dw_i -= L_q H_jl + U_q G_jr;  kind 1: L' = -L_q G_jl;
-// kind 2: U' = -U_q H_jr.  Column-major S x S complex, 64 x 64 tiles, 4 x 4 per thread.
+// One 64 x 64 tile (blockIdx.x, blockIdx.y) of Cm = [Cm] +- (A1 B1 + A2 B2) for
+// column-major S x S complex operands (A2 may be null), 4 x 4 outputs per thread,
+// FP64/FP32 CUDA cores.
 constexpr int kGT = 64, kGK = 16;
 template <typename C>
-__global__ void __launch_bounds__(256) k_even_gemm(FV<C> v, BcrLevel lv, int job0) {
+__device__ __forceinline__ void gemm_tile(const C *A1, const C *B1, const C *A2, const C *B2, C *Cm, int S,
+                                          bool accumulate, bool negate) {
     __shared__ C As[kGK][kGT + 1];
     __shared__ C Bs[kGK][kGT + 1];
-    const int S = v.S;
-    const int64_t SS = (int64_t)S * S;
-    const int job = job0 + blockIdx.z;
-    const int per = 3 * lv.neven;
-    const int64_t sh = job / per;
-    const int jj = job - (int)sh * per;
-    const int64_t e = jj / 3;
-    const int kind = jj - 3 * (int)e;
-    const int64_t q = 2 * e;
-    const bool hasl = q >= 1, hasr = q + 1 < lv.Kl;
-    const C *A1 = nullptr, *B1 = nullptr, *A2 = nullptr, *B2 = nullptr;
-    C *Cm = nullptr;
-    bool accumulate = false;
-    C *LU = v.LU + sh * v.lu_stride;
-    const C *G = v.G + sh * v.f_stride, *H = v.H + sh * v.f_stride;
-    const C *Lq = LU + (lv.lu_L + q) * SS, *Uq = LU + (lv.lu_U + q) * SS;
-    const int64_t jl = (q - 1) * lv.stride, jr = (q + 1) * lv.stride;
-    if (kind == 0) {
-        Cm = v.Dw + sh * v.f_stride + q * lv.stride * SS;
-        accumulate = true;
-        if (hasl) { A1 = Lq; B1 = H + jl * SS; }
-        if (hasr) { A2 = Uq; B2 = G + jr * SS; }
-    } else if (kind == 1) {
-        if (lv.lu_nL < 0 || q < 2) return;
-        Cm = LU + (lv.lu_nL + e) * SS;
-        A1 = Lq; B1 = G + jl * SS;
-    } else {
-        if (lv.lu_nU < 0 || q + 2 >= lv.Kl) return;
-        Cm = LU + (lv.lu_nU + e) * SS;
-        A1 = Uq; B1 = H + jr * SS;
-    }
     const int m0 = blockIdx.x * kGT, n0 = blockIdx.y * kGT;
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // 16 x 16 threads, 4 x 4 each
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // 16 x 16 threads
     C acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
@@ -499,9 +441,99 @@ __global__ void __launch_bounds__(256) k_even_gemm(FV<C> v, BcrLevel lv, int job
             const int gm = m0 + tx + 16 * a, gn = n0 + ty + 16 * b;
             if (gm < S && gn < S) {
                 const int64_t idx = gm + (int64_t)gn * S;
-                Cm[idx] = accumulate ? Cm[idx] - acc[a][b] : -acc[a][b];
+                const C d = negate ? -acc[a][b] : acc[a][b];
+                Cm[idx] = accumulate ? Cm[idx] + d : d;
             }
         }
+}
+
+// Batched dense update of the even blocks at levels >= 1 (complex128; the complex64
+// factorisation runs it on the tensor cores, gemm_tc.cu), one GEMM job per
+// (shift, even block, kind): kind 0: Dw_i -= L_q H_jl + U_q G_jr;  kind 1: L' = -L_q G_jl;
+// kind 2: U' = -U_q H_jr.
+template <typename C>
+__global__ void __launch_bounds__(256) k_even_gemm(FV<C> v, BcrLevel lv, int job0) {
+    const int S = v.S;
+    const int64_t SS = (int64_t)S * S;
+    const int job = job0 + blockIdx.z;
+    const int per = 3 * lv.neven;
+    const int64_t sh = job / per;
+    const int jj = job - (int)sh * per;
+    const int64_t e = jj / 3;
+    const int kind = jj - 3 * (int)e;
+    const int64_t q = 2 * e;
+    const bool hasl = q >= 1, hasr = q + 1 < lv.Kl;
+    const C *A1 = nullptr, *B1 = nullptr, *A2 = nullptr, *B2 = nullptr;
+    C *Cm = nullptr;
+    bool accumulate = false;
+    C *LU = v.LU + sh * v.lu_stride;
+    const C *G = v.G + sh * v.f_stride, *H = v.H + sh * v.f_stride;
+    const C *Lq = LU + (lv.lu_L + q) * SS, *Uq = LU + (lv.lu_U + q) * SS;
+    const int64_t jl = (q - 1) * lv.stride, jr = (q + 1) * lv.stride;
+    if (kind == 0) {
+        Cm = v.Dw + sh * v.f_stride + q * lv.stride * SS;
+        accumulate = true;
+        if (hasl) { A1 = Lq; B1 = H + jl * SS; }
+        if (hasr) { A2 = Uq; B2 = G + jr * SS; }
+    } else if (kind == 1) {
+        if (lv.lu_nL < 0 || q < 2) return;
+        Cm = LU + (lv.lu_nL + e) * SS;
+        A1 = Lq; B1 = G + jl * SS;
+    } else {
+        if (lv.lu_nU < 0 || q + 2 >= lv.Kl) return;
+        Cm = LU + (lv.lu_nU + e) * SS;
+        A1 = Uq; B1 = H + jr * SS;
+    }
+    if (!A1) { A1 = A2; B1 = B2; A2 = nullptr; B2 = nullptr; }
+    if (!A1) return;
+    gemm_tile<C>(A1, B1, A2, B2, Cm, S, accumulate, true);
+}
+
+// G_j = D_j^-1 L_q and H_j = D_j^-1 U_q of the odd blocks of a level >= 1 (complex128;
+// complex64 on the tensor cores), one job per (shift, odd block, G or H).
+template <typename C>
+__global__ void __launch_bounds__(256) k_gh_gemm(FV<C> v, BcrLevel lv, int job0) {
+    const int S = v.S;
+    const int64_t SS = (int64_t)S * S;
+    const int job = job0 + blockIdx.z;
+    const int64_t sh = job / (2 * lv.nodd);
+    const int jj = job - (int)sh * 2 * lv.nodd;
+    const int64_t o = jj / 2;
+    const int which = jj - 2 * (int)o;
+    const int64_t q = 2 * o + 1, j = q * lv.stride;
+    if (which == 1 && q + 1 >= lv.Kl) return;   // no right neighbour: H_j is never read
+    const C *Di = v.Dinv + sh * v.f_stride + j * SS;
+    const C *Bm = v.LU + sh * v.lu_stride + ((which ? lv.lu_U : lv.lu_L) + q) * SS;
+    C *Cm = (which ? v.H : v.G) + sh * v.f_stride + j * SS;
+    gemm_tile<C>(Di, Bm, nullptr, nullptr, Cm, S, false, false);
+}
+
+// Level 0: G_j = D_j^-1 (R L_j) and H_j = D_j^-1 (R U_j) from the couplings by column:
+// column c of G_j = sum over the entries (k, e) of column c of L_j of rs_k a_e D_j^-1[:, k]
+// (D_j^-1 is the inverse of the row-scaled block, so this is D^-1 L of the unscaled
+// system).  CTA = (chunk of kGhCW columns, odd index o, shift); one thread per row.
+constexpr int kGhCW = 8;
+template <typename C>
+__global__ void k_gh_l0(FV<C> v) {
+    const int S = v.S;
+    const int64_t SS = (int64_t)S * S;
+    const int64_t o = blockIdx.y, sh = blockIdx.z, j = 2 * o + 1;
+    const int c0 = blockIdx.x * kGhCW, c1 = min(S, c0 + kGhCW);
+    const C *Di = v.Dinv + sh * v.f_stride + j * SS;
+    const double *rs = v.rscale + sh * v.np + j * S;
+    for (int side = 0; side < 2; ++side) {
+        const int *ptr = v.cc_ptr + (2 * o + side) * (int64_t)(S + 1);
+        C *out = (side ? v.H : v.G) + sh * v.f_stride + j * SS;
+        for (int r = threadIdx.x; r < S; r += blockDim.x)
+            for (int c = c0; c < c1; ++c) {
+                C acc = czero<C>();
+                for (int t = ptr[c]; t < ptr[c + 1]; ++t) {
+                    const int k = v.cc_row[t];
+                    acc = cfma(acc, Di[r + (int64_t)k * S], from_c128<C>(rs[k] * v.aval[v.cc_src[t]]));
+                }
+                out[r + (int64_t)c * S] = acc;
+            }
+    }
 }
 
 constexpr int kUpdTW = 8;
@@ -522,22 +554,10 @@ int gauss_jordan(kore_plan *p, const FV<C> &v, const BcrLevel &lv, int nodd, int
         k_panel<C, NB><<<dim3(nodd, nshift), pthreads, smem, p->stream>>>(v, k0);
         KORE_LAUNCHED(1);
         const int cb = k0 + nb;
-        if (!top) {
-            // trailing columns: the rest of D, the L, U and identity columns
-            dim3 g(kore_div_up(4 * S - cb, kUpdTW), nodd, nshift);
-            k_update<C, NB, kUpdTW><<<g, 256, 0, p->stream>>>(v, k0, nb, cb, 4 * S);
-            KORE_LAUNCHED(1);
-        } else {
-            // the top block has no L, U columns: the rest of D, then the identity columns
-            if (cb < S) {
-                dim3 g(kore_div_up(S - cb, kUpdTW), nodd, nshift);
-                k_update<C, NB, kUpdTW><<<g, 256, 0, p->stream>>>(v, k0, nb, cb, S);
-                KORE_LAUNCHED(1);
-            }
-            dim3 g(kore_div_up(S, kUpdTW), nodd, nshift);
-            k_update<C, NB, kUpdTW><<<g, 256, 0, p->stream>>>(v, k0, nb, 3 * S, 4 * S);
-            KORE_LAUNCHED(1);
-        }
+        // trailing columns: the rest of D, then the identity columns
+        dim3 g(kore_div_up(2 * S - cb, kUpdTW), nodd, nshift);
+        k_update<C, NB, kUpdTW><<<g, 256, 0, p->stream>>>(v, k0, nb, cb, 2 * S);
+        KORE_LAUNCHED(1);
     }
     k_extract<C><<<grid_for((int64_t)nodd * S * S * nshift, 256, p->num_sms), 256, 0, p->stream>>>(v, lv, nodd, top,
                                                                                                 nshift);
@@ -558,39 +578,46 @@ int factor_levels(kore_plan *p) {
     KORE_LAUNCHED(2);
     for (int l = 0; l < p->nlev; ++l) {
         const BcrLevel &lv = p->lev[l];
-        k_T_fill<C><<<grid_for((int64_t)lv.nodd * 4 * SS * ns, 256, p->num_sms), 256, 0, st>>>(v, lv, lv.nodd, ns);
+        k_T_fill<C><<<grid_for((int64_t)lv.nodd * 2 * SS * ns, 256, p->num_sms), 256, 0, st>>>(v, lv, lv.nodd, ns);
         KORE_LAUNCHED(1);
-        if (l == 0) {
-            k_T_scatter_LU<C><<<grid_for((int64_t)lv.nodd * S * 32 * ns, 256, p->num_sms), 256, 0, st>>>(v, lv.nodd,
-                                                                                                        ns);
-            KORE_LAUNCHED(1);
-        }
+        // D_j^-1 of the odd blocks by Gauss-Jordan on [D_j | I]
         KORE_TRY((gauss_jordan<C, NB>(p, v, lv, lv.nodd, 0, ns)));
+        const int th = std::min(1024, ((S + 31) / 32) * 32);
         if (l == 0) {
+            // G_j, H_j from the sparse couplings (complex64: refined on the tensor cores),
+            // then the even blocks
+            k_gh_l0<C><<<dim3(kore_div_up(S, kGhCW), lv.nodd, ns), th, 0, st>>>(v);
+            KORE_LAUNCHED(1);
+            if (sizeof(C) == sizeof(float2)) KORE_TRY(kore_gh_update_tc(p, lv, 1));
             dim3 g(kore_div_up(S, kEvenCW), lv.neven, ns);
-            const int th = std::min(1024, ((S + 31) / 32) * 32);
             k_even_l0<C><<<g, th, 0, st>>>(v, lv);
             KORE_LAUNCHED(1);
         } else if (sizeof(C) == sizeof(float2)) {
             // complex64: tensor cores (3xTF32)
+            KORE_TRY(kore_gh_update_tc(p, lv, 0));
             KORE_TRY(kore_even_update_tc(p, lv));
         } else {
             // complex128: FP64 CUDA cores
+            const dim3 tg(kore_div_up(S, kGT), kore_div_up(S, kGT));
+            const int gjobs = 2 * lv.nodd * ns;
+            for (int j0 = 0; j0 < gjobs; j0 += 65535) {
+                k_gh_gemm<C><<<dim3(tg.x, tg.y, std::min(65535, gjobs - j0)), 256, 0, st>>>(v, lv, j0);
+                KORE_LAUNCHED(1);
+            }
             const int jobs = 3 * lv.neven * ns;
             for (int j0 = 0; j0 < jobs; j0 += 65535) {
-                dim3 g(kore_div_up(S, kGT), kore_div_up(S, kGT), std::min(65535, jobs - j0));
-                k_even_gemm<C><<<g, 256, 0, st>>>(v, lv, j0);
+                k_even_gemm<C><<<dim3(tg.x, tg.y, std::min(65535, jobs - j0)), 256, 0, st>>>(v, lv, j0);
                 KORE_LAUNCHED(1);
             }
         }
         KORE_CUDA_TRY(cudaGetLastError());
     }
-    // the last active block (block 0): T = [Dw_0 | 0 | 0 | I]; stride 0 maps odd index 0 to block 0
+    // the last active block (block 0): T = [Dw_0 | I]; stride 0 maps odd index 0 to block 0
     BcrLevel top{};
     top.Kl = 1;
     top.stride = 0;
     top.lu_L = top.lu_U = top.lu_nL = top.lu_nU = -1;
-    k_T_fill<C><<<grid_for(4 * SS * ns, 256, p->num_sms), 256, 0, st>>>(v, top, 1, ns);
+    k_T_fill<C><<<grid_for(2 * SS * ns, 256, p->num_sms), 256, 0, st>>>(v, top, 1, ns);
     KORE_LAUNCHED(1);
     KORE_TRY((gauss_jordan<C, NB>(p, v, top, 1, 1, ns)));
     return KORE_OK;

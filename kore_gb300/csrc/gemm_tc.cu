@@ -360,15 +360,20 @@ __global__ void k_tc_fill(float2 *x, int64_t n, uint64_t seed) {
 }  // namespace
 
 // ----------------------------------------------------------------------------- factorisation use
+int tc_upload_run(kore_plan *p, const std::vector<const float2 *> &src, int64_t nA, const std::vector<TcJob> &jobs);
 // Bytes of the split planes and the job table for one reduction level's even-block update
 // (levels >= 1) of `cap` shifts; the plan allocates the largest over its levels.
 void kore_tc_level_bytes(const kore_plan *p, int cap, int64_t *plane_bytes, int64_t *table_bytes) {
     int64_t pl = 0, tb = 0;
     const int64_t S = p->S, Kp = tc_kp(p->S);
-    for (int l = 1; l < p->nlev; ++l) {
-        const int64_t nm = 2 * (int64_t)(p->lev[l].neven + p->lev[l].nodd) * cap;
+    for (int l = 0; l < p->nlev; ++l) {
+        const int64_t ne = p->lev[l].neven, no = p->lev[l].nodd;
+        // even update (levels >= 1): 2 neven A + 2 nodd B matrices, 3 neven jobs;
+        // G, H and their refinement (every level): nodd A + 2 nodd B matrices, 2 nodd jobs
+        const int64_t nm = std::max(l > 0 ? 2 * (ne + no) : 0, 3 * no) * cap;
+        const int64_t nj = std::max(l > 0 ? 3 * ne : 0, 2 * no) * cap;
         pl = std::max(pl, nm * 4 * S * Kp * 4);
-        tb = std::max(tb, nm * 8 + 3 * (int64_t)p->lev[l].neven * cap * (int64_t)sizeof(TcJob) + 64);
+        tb = std::max(tb, nm * 8 + nj * (int64_t)sizeof(TcJob) + 64);
     }
     *plane_bytes = pl;
     *table_bytes = tb;
@@ -422,15 +427,116 @@ int kore_even_update_tc(kore_plan *p, const BcrLevel &lv) {
                 jobs.push_back(TcJob{aU, br + 1, -1, -1, LU + (lv.lu_nU + e) * SS, -1.f, 0});
         }
     }
-    // table: pointers (8-byte aligned), then jobs
+    (void)nB;
+    return tc_upload_run(p, src, nA, jobs);
+}
+
+// R(k, c) += rs_k a_e for the level-0 couplings of the odd blocks (side 0: L_j into
+// R_G, side 1: U_j into R_H), R_G and R_H at Rbase + shift * t_stride + o * 2 S^2 (+ S^2).
+// CTA = (odd index o, side, shift); threads over the columns.
+__global__ void k_add_couplings(const int *__restrict__ cc_ptr, const int *__restrict__ cc_row,
+                                const int *__restrict__ cc_src, const double2 *__restrict__ aval,
+                                const double *__restrict__ rscale, int S, int64_t np, float2 *Rbase,
+                                int64_t t_stride) {
+    const int64_t o = blockIdx.x, side = blockIdx.y, sh = blockIdx.z;
+    const int64_t SS = (int64_t)S * S, j = 2 * o + 1;
+    const int *ptr = cc_ptr + (2 * o + side) * (int64_t)(S + 1);
+    const double *rs = rscale + sh * np + j * S;
+    float2 *R = Rbase + sh * t_stride + o * 2 * SS + side * SS;
+    for (int c = threadIdx.x; c < S; c += blockDim.x)
+        for (int t = ptr[c]; t < ptr[c + 1]; ++t) {
+            const int k = cc_row[t];
+            const double2 a = rs[k] * aval[cc_src[t]];
+            float2 &r = R[k + (int64_t)c * S];
+            r = make_float2((float)((double)r.x + a.x), (float)((double)r.y + a.y));
+        }
+}
+
+int tc_upload_run(kore_plan *p, const std::vector<const float2 *> &src, int64_t nA, const std::vector<TcJob> &jobs) {
     const size_t pbytes = src.size() * sizeof(void *), jbytes = jobs.size() * sizeof(TcJob);
     unsigned char *tab = static_cast<unsigned char *>(p->d_tctab);
     KORE_CUDA_TRY(cudaMemcpyAsync(tab, src.data(), pbytes, cudaMemcpyHostToDevice, p->stream));
     KORE_CUDA_TRY(cudaMemcpyAsync(tab + pbytes, jobs.data(), jbytes, cudaMemcpyHostToDevice, p->stream));
     const float2 *const *dsrc = reinterpret_cast<const float2 *const *>(tab);
-    return tc_run(p->stream, p->device, S, dsrc, (int)nA, dsrc + nA, (int)nB,
+    return tc_run(p->stream, p->device, p->S, dsrc, (int)nA, dsrc + nA, (int)(src.size() - nA),
                   reinterpret_cast<const TcJob *>(tab + pbytes), (int)jobs.size(), static_cast<float *>(p->d_tcplanes),
                   p->d_err);
+}
+
+// G_j = D_j^-1 L_j and H_j = D_j^-1 U_j of the odd blocks of a level for every shift
+// (complex64 factors), on the tensor cores, with one step of refinement:
+//     G0 = D^-1 L,   R = L - D G0,   G = G0 + D^-1 R
+// (D is the row-scaled diagonal block, D^-1 its Gauss-Jordan inverse).  The product with
+// an explicit inverse loses accuracy where D^-1 L cancels; the refinement step gives
+// the columns of G the accuracy of a stable solve, which keeps the FP64 refinement of
+// the solves at two to three corrections.  Level >= 1: dense L, U in the coupling
+// store (the odd blocks' L, U are not read again, so R overwrites them).  Level 0:
+// G0 and H0 come from the sparse couplings (k_gh_l0); R goes to the Gauss-Jordan work
+// area T, free after the extraction.
+int kore_gh_update_tc(kore_plan *p, const BcrLevel &lv, int level0) {
+    const int S = p->S, ns = p->nshift;
+    const int64_t SS = (int64_t)S * S, no = lv.nodd;
+    float2 *Dinv = static_cast<float2 *>(p->d_Dinv), *Dw = static_cast<float2 *>(p->d_Dw);
+    float2 *G = static_cast<float2 *>(p->d_Gm), *H = static_cast<float2 *>(p->d_Hm);
+    float2 *LU = static_cast<float2 *>(p->d_LU), *T = static_cast<float2 *>(p->d_T);
+    auto blk = [&](float2 *base, int sh, int64_t o) { return base + sh * p->f_stride() + (2 * o + 1) * lv.stride * SS; };
+    // residual storage of (shift, odd o, side)
+    auto rstore = [&](int sh, int64_t o, int side) -> float2 * {
+        if (level0) return T + sh * p->t_stride() + o * 2 * SS + side * SS;
+        return LU + sh * p->lu_stride() + ((side ? lv.lu_U : lv.lu_L) + 2 * o + 1) * SS;
+    };
+    auto hasr = [&](int64_t o) { return 2 * o + 2 < lv.Kl; };
+    std::vector<const float2 *> src;
+    std::vector<TcJob> jobs;
+    // stage 1 (levels >= 1): G0 = D^-1 L, H0 = D^-1 U
+    if (!level0) {
+        for (int sh = 0; sh < ns; ++sh)
+            for (int64_t o = 0; o < no; ++o) src.push_back(blk(Dinv, sh, o));
+        for (int sh = 0; sh < ns; ++sh)
+            for (int64_t o = 0; o < no; ++o) { src.push_back(rstore(sh, o, 0)); src.push_back(rstore(sh, o, 1)); }
+        for (int sh = 0; sh < ns; ++sh)
+            for (int64_t o = 0; o < no; ++o) {
+                const int a = (int)(sh * no + o);
+                jobs.push_back(TcJob{a, 2 * a, -1, -1, blk(G, sh, o), 1.f, 0});
+                if (hasr(o)) jobs.push_back(TcJob{a, 2 * a + 1, -1, -1, blk(H, sh, o), 1.f, 0});
+            }
+        KORE_TRY(tc_upload_run(p, src, ns * no, jobs));
+    }
+    // stage 2: R = L - D G0 (level 0: R = -D G0, then + L from the sparse couplings)
+    src.clear();
+    jobs.clear();
+    for (int sh = 0; sh < ns; ++sh)
+        for (int64_t o = 0; o < no; ++o) src.push_back(blk(Dw, sh, o));
+    for (int sh = 0; sh < ns; ++sh)
+        for (int64_t o = 0; o < no; ++o) { src.push_back(blk(G, sh, o)); src.push_back(blk(H, sh, o)); }
+    for (int sh = 0; sh < ns; ++sh)
+        for (int64_t o = 0; o < no; ++o) {
+            const int a = (int)(sh * no + o);
+            const int beta = level0 ? 0 : 1;
+            jobs.push_back(TcJob{a, 2 * a, -1, -1, rstore(sh, o, 0), -1.f, beta});
+            if (hasr(o)) jobs.push_back(TcJob{a, 2 * a + 1, -1, -1, rstore(sh, o, 1), -1.f, beta});
+        }
+    KORE_TRY(tc_upload_run(p, src, ns * no, jobs));
+    if (level0) {
+        k_add_couplings<<<dim3((unsigned)no, 2, ns), 256, 0, p->stream>>>(p->d_cc_ptr, p->d_cc_row, p->d_cc_src,
+                                                                          p->d_aval, p->d_rscale, S, p->np, T,
+                                                                          p->t_stride());
+        KORE_LAUNCHED(1);
+    }
+    // stage 3: G = G0 + D^-1 R
+    src.clear();
+    jobs.clear();
+    for (int sh = 0; sh < ns; ++sh)
+        for (int64_t o = 0; o < no; ++o) src.push_back(blk(Dinv, sh, o));
+    for (int sh = 0; sh < ns; ++sh)
+        for (int64_t o = 0; o < no; ++o) { src.push_back(rstore(sh, o, 0)); src.push_back(rstore(sh, o, 1)); }
+    for (int sh = 0; sh < ns; ++sh)
+        for (int64_t o = 0; o < no; ++o) {
+            const int a = (int)(sh * no + o);
+            jobs.push_back(TcJob{a, 2 * a, -1, -1, blk(G, sh, o), 1.f, 1});
+            if (hasr(o)) jobs.push_back(TcJob{a, 2 * a + 1, -1, -1, blk(H, sh, o), 1.f, 1});
+        }
+    return tc_upload_run(p, src, ns * no, jobs);
 }
 
 extern "C" int kore_tc_selftest(int device, int S, int nmat, double *max_rel_err) {

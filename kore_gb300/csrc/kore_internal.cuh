@@ -90,7 +90,7 @@ struct kore_plan {
     // S x S column-major blocks, indexed by original block number, per shift
     void *d_Dinv = nullptr, *d_Gm = nullptr, *d_Hm = nullptr, *d_Dw = nullptr;
     void *d_LU = nullptr;             // lu_mats blocks per shift
-    void *d_T = nullptr;              // nodd_max x (S x 4S) Gauss-Jordan work per shift, column-major
+    void *d_T = nullptr;              // nodd_max x (S x 2S) Gauss-Jordan work [D | I] per shift, column-major
     double *d_rscale = nullptr;       // np row equilibration factors per shift
     int *d_piv = nullptr;             // nodd_max x S per shift: pivot row chosen for column k
     int *d_pidx = nullptr;            // nodd_max x S per shift: position of a row in the current panel or -1
@@ -101,6 +101,12 @@ struct kore_plan {
     int ell_w = 0;                    // padded width (multiple of 8) of a coupling row
     int64_t ell_rows = 0;             // even blocks of level 0 x ntile x 32
     int64_t ell_nnz = 0;              // coupling entries (without the padding)
+    // Level-0 couplings of the odd blocks j (rows of block j, columns of block j-1 for
+    // side 0 and of block j+1 for side 1) by column, for G_j = D_j^-1 L_j and
+    // H_j = D_j^-1 U_j: column c of (odd index o, side) holds the entries
+    // [cc_ptr[(2 o + side) (S + 1) + c], ... + c + 1) with row k in the block (cc_row)
+    // and the entry of A in the permuted CSR (cc_src).
+    int *d_cc_ptr = nullptr, *d_cc_row = nullptr, *d_cc_src = nullptr;
     int *d_ell_col = nullptr;         // padded slot of the coupled unknown, -1 for padding
     int *d_ell_src = nullptr;         // entry of A in the permuted CSR, -1 for padding
     void *d_ell_val = nullptr;        // per shift: rscale_row * A entry, factor precision
@@ -111,7 +117,7 @@ struct kore_plan {
 
     int64_t f_stride() const { return (int64_t)K * S * S; }
     int64_t lu_stride() const { return lu_mats * (int64_t)S * S; }
-    int64_t t_stride() const { return (int64_t)nodd_max * 4 * S * S; }
+    int64_t t_stride() const { return (int64_t)nodd_max * 2 * S * S; }
     int64_t p_stride() const { return (int64_t)nodd_max * S; }
     int64_t ell_stride() const { return ell_rows * ell_w; }
 
@@ -168,6 +174,9 @@ int kore_factor_impl(kore_plan *p, int nshift, const double *sigmas, int precisi
 
 // gemm_tc.cu: tensor-core (tcgen05, 3xTF32) even-block update of a level >= 1, complex64
 int kore_even_update_tc(kore_plan *p, const BcrLevel &lv);
+// G_j, H_j of the odd blocks with one refinement step (level0: G0, H0 already formed
+// from the sparse couplings)
+int kore_gh_update_tc(kore_plan *p, const BcrLevel &lv, int level0);
 void kore_tc_level_bytes(const kore_plan *p, int cap, int64_t *plane_bytes, int64_t *table_bytes);
 
 // sweep.cu

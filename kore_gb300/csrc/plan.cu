@@ -98,7 +98,7 @@ void free_plan(kore_plan *p) {
                     p->d_red, p->d_part, p->d_err, p->d_bar, p->d_ir, p->d_V, p->d_Vtmp, p->d_small,
                     p->d_sigma, p->d_minf, p->d_bb, p->d_xb, p->d_rb, p->d_bn, p->d_rn, p->d_cnt,
                     p->d_ell_col, p->d_ell_src, p->d_ell_val, p->d_long_rows, p->d_srow, p->d_smid,
-                    p->d_scol, p->d_sval};
+                    p->d_scol, p->d_sval, p->d_cc_ptr, p->d_cc_row, p->d_cc_src};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     for (auto &v : p->d_v)
@@ -188,6 +188,29 @@ int build_ell(kore_plan *p, const std::vector<int> &row, const std::vector<int> 
         }
     KORE_TRY(upload(p, &p->d_ell_col, ecol));
     KORE_TRY(upload(p, &p->d_ell_src, esrc));
+    // the odd blocks' couplings by column (G_j = D_j^-1 L_j, H_j = D_j^-1 U_j at level 0)
+    const int64_t no = p->nlev > 0 ? p->lev[0].nodd : 0;
+    std::vector<int> cptr(std::max<int64_t>(2 * no * (S + 1), 1), 0), crow, csrc;
+    for (int64_t o = 0; o < no; ++o)
+        for (int side = 0; side < 2; ++side) {
+            const int64_t j = 2 * o + 1, nbr = side ? j + 1 : j - 1;
+            std::vector<std::vector<std::pair<int, int>>> bycol(S);
+            for (int64_t r = 0; r < S; ++r) {
+                const int64_t q = j * S + r;
+                const int e0 = side ? split[2 * q + 1] : row[q], e1 = side ? row[q + 1] : split[2 * q];
+                for (int e = e0; e < e1; ++e) bycol[col[e] - nbr * S].push_back({(int)r, e});
+            }
+            int *ptr = &cptr[(2 * o + side) * (S + 1)];
+            ptr[0] = (int)crow.size();
+            for (int64_t c = 0; c < S; ++c) {
+                for (const auto &re : bycol[c]) { crow.push_back(re.first); csrc.push_back(re.second); }
+                ptr[c + 1] = (int)crow.size();
+            }
+        }
+    if (crow.empty()) { crow.push_back(0); csrc.push_back(0); }
+    KORE_TRY(upload(p, &p->d_cc_ptr, cptr));
+    KORE_TRY(upload(p, &p->d_cc_row, crow));
+    KORE_TRY(upload(p, &p->d_cc_src, csrc));
     return KORE_OK;
 }
 
@@ -504,7 +527,19 @@ int kore_plan_estimate_bytes(const kore_pencil_desc *d, int precision, int nshif
     b += (np + 1) * 4 + nb * 12;
     b += np * 8 + K * 4 + nlev * (int64_t)sizeof(BcrLevel) + 6 * np * 16 + 8192 * 8 + 1024;
     // factors and solve workspace of c shifts
-    b += c * (4 * K * SS * e + lu * SS * e + nodd_max * 4 * SS * e + 3 * np * e + np * 8 + 3 * nodd_max * S * 4);
+    b += c * (4 * K * SS * e + lu * SS * e + nodd_max * 2 * SS * e + 3 * np * e + np * 8 + 3 * nodd_max * S * 4);
+    // level-0 couplings by column; split planes and job table of the tensor-core updates
+    b += (2 * (K / 2 + 1) * (S + 1) + 2 * na) * 4;
+    if (precision == KORE_PREC_MIXED) {
+        const int64_t Kp = (S + 31) / 32 * 32;
+        int64_t nm = 0, nj = 0;
+        for (int64_t l = 0; l < nlev; ++l) {
+            const int64_t ne = Ks[l] - Ks[l] / 2, no = Ks[l] / 2;
+            nm = std::max<int64_t>(nm, std::max<int64_t>(l > 0 ? 2 * Ks[l] : 0, 3 * no));
+            nj = std::max<int64_t>(nj, std::max<int64_t>(l > 0 ? 3 * ne : 0, 2 * no));
+        }
+        b += c * (nm * 4 * S * Kp * 4 + nm * 8 + nj * 32 + 64);
+    }
     b += c * (3 * np * 16 + 2 * (np / 64 + np / 8 + 1024) * 8 + (3 * nlev + 1) * K * 4 + ell * e + 128);
     b += 2 * d->n * c * 16;   // kore_solve's device copies of b and x
     // Krylov basis, its copy and the projected-problem workspace

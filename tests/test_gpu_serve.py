@@ -83,7 +83,7 @@ def test_admission_under_a_small_budget(gpu_lib, case):
         for rep in range(2):
             for m, A, B, P in datas:
                 b = rng.standard_normal(P.n) + 1j * rng.standard_normal(P.n)
-                ts.append((srv.submit_forced(P, 0.2j * (rep + 1), b), A, B, b, 0.2j * (rep + 1)))
+                ts.append((srv.submit_forced(P, 0.2j * (rep + 1), b, refine_tol=1e-15), A, B, b, 0.2j * (rep + 1)))
         for t, A, B, b, s in ts:
             r = srv.result(t)
             assert solve_residual((A - s * B).tocsr(), r["x"], b) < 1e-14
