@@ -59,34 +59,6 @@ struct SchurOut {
     int *info;        // 0 ok, 1 QR failed to converge
 };
 
-// Givens rotation G = [c s; -conj(s) c] with G [x; y] = [r; 0]
-__device__ inline void givens(double2 x, double2 y, double &c, double2 &s) {
-    const double ax = sqrt(abs2(x)), ay = sqrt(abs2(y));
-    if (ay == 0.0) { c = 1.0; s = mk(0.0, 0.0); return; }
-    if (ax == 0.0) { c = 0.0; s = mk(1.0, 0.0); return; }
-    const double nrm = hypot(ax, ay);
-    c = ax / nrm;
-    const double2 u = mk(x.x / ax, x.y / ax);
-    s = (1.0 / nrm) * (u * conjg(y));
-}
-
-// rows k,k+1 of M (ld) over columns [c0, c1): [a; b] <- [c a + s b; -conj(s) a + c b]
-__device__ inline void rot_rows(double2 *M, int ld, int k, int c0, int c1, double c, double2 s) {
-    for (int j = c0 + threadIdx.x; j < c1; j += blockDim.x) {
-        const double2 a = M[k + j * ld], b = M[k + 1 + j * ld];
-        M[k + j * ld] = c * a + s * b;
-        M[k + 1 + j * ld] = c * b - conjg(s) * a;
-    }
-}
-// columns k,k+1 of M over rows [r0, r1): [a, b] <- [a c + b conj(s), -a s + b c]
-__device__ inline void rot_cols(double2 *M, int ld, int k, int r0, int r1, double c, double2 s) {
-    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        const double2 a = M[i + k * ld], b = M[i + (k + 1) * ld];
-        M[i + k * ld] = c * a + b * conjg(s);
-        M[i + (k + 1) * ld] = c * b - a * s;
-    }
-}
-
 __device__ inline double cabs_(double2 a) { return hypot(a.x, a.y); }
 
 __device__ inline double2 csqrt_(double2 z) {
@@ -112,14 +84,30 @@ __device__ __forceinline__ void givens_r(double2 x, double2 y, double &c, double
 
 // Apply G from the left to rows k, k+1 and G^H from the right to columns k, k+1 of H
 // (rows [0, r1), columns [c0, m)), and G^H to columns k, k+1 of Q, in one parallel step.
-// The 2 x 2 block where the row and column updates meet is done by one thread.
+// The FP64 dependency chain of a rotation is its latency (about 64 cycles per FP64
+// operation on this GPU), so the 2 x 2 block where the row and column updates meet is
+// split over lanes 0-3 of the last warp, one entry each, while the other warps update
+// every other entry (one per thread): the two run on different SM sub-partitions.
 __device__ __forceinline__ void apply_rot(double2 *H, double2 *Q, int m, int k, int c0, int r1, double c, double2 s) {
-    const int tid = threadIdx.x, nt = blockDim.x;
+    const int tid = threadIdx.x, nt = blockDim.x - 32;
+    if (tid >= nt) {
+        if (tid >= nt + 4) return;
+        const double2 h00 = H[k + k * m], h01 = H[k + (k + 1) * m], h10 = H[k + 1 + k * m],
+                      h11 = H[k + 1 + (k + 1) * m];
+        const int r = tid & 1, cc = (tid >> 1) & 1;   // output row k + r, column k + cc
+        // rows of G [h]: row r of the rotated rows, at columns k and k+1
+        const double2 ta = r ? c * h10 - conjg(s) * h00 : c * h00 + s * h10;   // column k
+        const double2 tb = r ? c * h11 - conjg(s) * h01 : c * h01 + s * h11;   // column k+1
+        const double2 out = cc ? c * tb - ta * s : c * ta + tb * conjg(s);
+        __syncwarp(0xFu);
+        H[k + r + (k + cc) * m] = out;
+        return;
+    }
     const int nrow = m - (k + 2);                     // columns k+2.. of rows k, k+1
     const int ncol = (r1 > k) ? k : r1;                // rows 0..k-1 of columns k, k+1
     const int nlow = (r1 > k + 2) ? 1 : 0;             // row k+2 of columns k, k+1
     const int nleft = (c0 < k) ? 1 : 0;                // column k-1 of rows k, k+1
-    const int total = nrow + ncol + nlow + nleft + m + 1;
+    const int total = nrow + ncol + nlow + nleft + m;
     for (int t = tid; t < total; t += nt) {
         int u = t;
         if (u < nrow) {
@@ -146,20 +134,9 @@ __device__ __forceinline__ void apply_rot(double2 *H, double2 *Q, int m, int k, 
             continue;
         }
         u -= nleft;
-        if (u < m) {
-            const double2 a = Q[u + k * m], b = Q[u + (k + 1) * m];
-            Q[u + k * m] = c * a + b * conjg(s);
-            Q[u + (k + 1) * m] = c * b - a * s;
-            continue;
-        }
-        // the 2 x 2 block: rows then columns
-        double2 h00 = H[k + k * m], h01 = H[k + (k + 1) * m], h10 = H[k + 1 + k * m], h11 = H[k + 1 + (k + 1) * m];
-        double2 t00 = c * h00 + s * h10, t01 = c * h01 + s * h11;
-        double2 t10 = c * h10 - conjg(s) * h00, t11 = c * h11 - conjg(s) * h01;
-        H[k + k * m] = c * t00 + t01 * conjg(s);
-        H[k + (k + 1) * m] = c * t01 - t00 * s;
-        H[k + 1 + k * m] = c * t10 + t11 * conjg(s);
-        H[k + 1 + (k + 1) * m] = c * t11 - t10 * s;
+        const double2 a = Q[u + k * m], b = Q[u + (k + 1) * m];
+        Q[u + k * m] = c * a + b * conjg(s);
+        Q[u + (k + 1) * m] = c * b - a * s;
     }
 }
 

@@ -55,6 +55,10 @@ struct FV {
     C *Dinv, *G, *H, *Dw, *LU, *T;
     int *piv, *pidx, *used, *err;
     const int *cc_ptr, *cc_row, *cc_src;
+    const int *ell_col;      // level-0 coupling rows of the even blocks (kore_plan::d_ell_*)
+    const C *ell_val;
+    int ell_w;
+    int64_t ell_stride;
     int64_t f_stride, lu_stride, t_stride, p_stride;
 };
 
@@ -69,6 +73,8 @@ FV<C> make_fv(kore_plan *p) {
     v.Dw = static_cast<C *>(p->d_Dw); v.LU = static_cast<C *>(p->d_LU); v.T = static_cast<C *>(p->d_T);
     v.piv = p->d_piv; v.pidx = p->d_pidx; v.used = p->d_used; v.err = p->d_err;
     v.cc_ptr = p->d_cc_ptr; v.cc_row = p->d_cc_row; v.cc_src = p->d_cc_src;
+    v.ell_col = p->d_ell_col; v.ell_val = static_cast<const C *>(p->d_ell_val); v.ell_w = p->ell_w;
+    v.ell_stride = p->ell_stride();
     v.f_stride = p->f_stride(); v.lu_stride = p->lu_stride(); v.t_stride = p->t_stride(); v.p_stride = p->p_stride();
     return v;
 }
@@ -343,49 +349,63 @@ __global__ void k_extract(FV<C> v, BcrLevel lv, int nodd, int top, int nshift) {
     }
 }
 
-// Level 0 update of the even blocks with the sparse couplings of the CSR:
+// Level 0 update of the even blocks with their sparse couplings:
 //   Dw_i -= rs (L_i H_jl + U_i G_jr),  L'_i = -rs L_i G_jl,  U'_i = -rs U_i H_jr.
-// CTA = (chunk of CW columns, even index e, shift); one thread per row.
+// CTA = (chunk of kEvenCW columns, even index e, shift); one thread per row, which reads
+// its row's coupling entries once, as padded rows (the level-0 rows of the sweep, with
+// the row scale folded in), and accumulates the kEvenCW columns in registers.
 constexpr int kEvenCW = 8;
 template <typename C>
-__global__ void k_even_l0(FV<C> v, BcrLevel lv) {
+__global__ void __launch_bounds__(512) k_even_l0(FV<C> v, BcrLevel lv) {
     const int S = v.S;
     const int64_t SS = (int64_t)S * S;
     const int64_t e = blockIdx.y, sh = blockIdx.z;
     const int64_t q = 2 * e;                 // position = original block at level 0
-    const bool hasl = q >= 1, hasr = q + 1 < lv.Kl;
     const bool outl = (lv.lu_nL >= 0) && q >= 2, outr = (lv.lu_nU >= 0) && q + 2 < lv.Kl;
     const int c0 = blockIdx.x * kEvenCW;
     const int cn = min(kEvenCW, S - c0);
+    const int ntile = (S + 31) / 32;
     C *Di = v.Dw + sh * v.f_stride + q * SS;
     const C *G = v.G + sh * v.f_stride, *H = v.H + sh * v.f_stride;
+    const C *Hl = H + (q - 1) * SS, *Gl = G + (q - 1) * SS, *Gr = G + (q + 1) * SS, *Hr = H + (q + 1) * SS;
     C *LU = v.LU + sh * v.lu_stride;
-    const double *rscale = v.rscale + sh * v.np;
+    const C *ev = v.ell_val + sh * v.ell_stride;
     for (int r = threadIdx.x; r < S; r += blockDim.x) {
-        const int64_t p = q * S + r;
-        const int l0 = v.arow[p], l1 = v.asplit[2 * p], u0 = v.asplit[2 * p + 1], u1 = v.arow[p + 1];
-        const double rs = rscale[p];
-        for (int t = 0; t < cn; ++t) {
-            const int64_t col = (int64_t)(c0 + t) * S;
-            C dsum = czero<C>(), lsum = czero<C>(), usum = czero<C>();
-            if (hasl)
-                for (int k = l0; k < l1; ++k) {
-                    const C a = from_c128<C>(rs * v.aval[k]);
-                    const int64_t cr = v.acol[k] - (q - 1) * S;
-                    dsum = cfma(dsum, a, H[(q - 1) * SS + cr + col]);
-                    if (outl) lsum = cfma(lsum, a, G[(q - 1) * SS + cr + col]);
-                }
-            if (hasr)
-                for (int k = u0; k < u1; ++k) {
-                    const C a = from_c128<C>(rs * v.aval[k]);
-                    const int64_t cr = v.acol[k] - (q + 1) * S;
-                    dsum = cfma(dsum, a, G[(q + 1) * SS + cr + col]);
-                    if (outr) usum = cfma(usum, a, H[(q + 1) * SS + cr + col]);
-                }
-            Di[r + col] = Di[r + col] - dsum;
-            if (outl) LU[(lv.lu_nL + e) * SS + r + col] = -lsum;
-            if (outr) LU[(lv.lu_nU + e) * SS + r + col] = -usum;
+        C dsum[kEvenCW], lsum[kEvenCW], usum[kEvenCW];
+#pragma unroll
+        for (int t = 0; t < kEvenCW; ++t) dsum[t] = lsum[t] = usum[t] = czero<C>();
+        const int64_t ebase = ((e * ntile + r / 32) * (int64_t)v.ell_w) * 32 + (r & 31);
+        for (int k = 0; k < v.ell_w; ++k) {
+            const int col = v.ell_col[ebase + (int64_t)k * 32];
+            if (col < 0) continue;
+            const C a = ev[ebase + (int64_t)k * 32];
+            const int64_t blk = col / S, cr = col - blk * S;
+            if (blk < q) {   // left neighbour j = q - 1
+#pragma unroll
+                for (int t = 0; t < kEvenCW; ++t)
+                    if (t < cn) {
+                        const int64_t o = cr + (int64_t)(c0 + t) * S;
+                        dsum[t] = cfma(dsum[t], a, Hl[o]);
+                        if (outl) lsum[t] = cfma(lsum[t], a, Gl[o]);
+                    }
+            } else {         // right neighbour j = q + 1
+#pragma unroll
+                for (int t = 0; t < kEvenCW; ++t)
+                    if (t < cn) {
+                        const int64_t o = cr + (int64_t)(c0 + t) * S;
+                        dsum[t] = cfma(dsum[t], a, Gr[o]);
+                        if (outr) usum[t] = cfma(usum[t], a, Hr[o]);
+                    }
+            }
         }
+#pragma unroll
+        for (int t = 0; t < kEvenCW; ++t)
+            if (t < cn) {
+                const int64_t col = (int64_t)(c0 + t) * S;
+                Di[r + col] = Di[r + col] - dsum[t];
+                if (outl) LU[(lv.lu_nL + e) * SS + r + col] = -lsum[t];
+                if (outr) LU[(lv.lu_nU + e) * SS + r + col] = -usum[t];
+            }
     }
 }
 
@@ -511,10 +531,14 @@ __global__ void __launch_bounds__(256) k_gh_gemm(FV<C> v, BcrLevel lv, int job0)
 // Level 0: G_j = D_j^-1 (R L_j) and H_j = D_j^-1 (R U_j) from the couplings by column:
 // column c of G_j = sum over the entries (k, e) of column c of L_j of rs_k a_e D_j^-1[:, k]
 // (D_j^-1 is the inverse of the row-scaled block, so this is D^-1 L of the unscaled
-// system).  CTA = (chunk of kGhCW columns, odd index o, shift); one thread per row.
+// system).  CTA = (chunk of kGhCW columns, odd index o, shift): the entries of one column
+// are staged in shared memory, then one thread per row accumulates.
 constexpr int kGhCW = 8;
+constexpr int kGhBuf = 512;
 template <typename C>
-__global__ void k_gh_l0(FV<C> v) {
+__global__ void __launch_bounds__(512) k_gh_l0(FV<C> v) {
+    __shared__ int sk[kGhBuf];
+    __shared__ C sv[kGhBuf];
     const int S = v.S;
     const int64_t SS = (int64_t)S * S;
     const int64_t o = blockIdx.y, sh = blockIdx.z, j = 2 * o + 1;
@@ -524,15 +548,30 @@ __global__ void k_gh_l0(FV<C> v) {
     for (int side = 0; side < 2; ++side) {
         const int *ptr = v.cc_ptr + (2 * o + side) * (int64_t)(S + 1);
         C *out = (side ? v.H : v.G) + sh * v.f_stride + j * SS;
-        for (int r = threadIdx.x; r < S; r += blockDim.x)
-            for (int c = c0; c < c1; ++c) {
-                C acc = czero<C>();
-                for (int t = ptr[c]; t < ptr[c + 1]; ++t) {
-                    const int k = v.cc_row[t];
-                    acc = cfma(acc, Di[r + (int64_t)k * S], from_c128<C>(rs[k] * v.aval[v.cc_src[t]]));
+        for (int c = c0; c < c1; ++c) {
+            C acc[4] = {czero<C>(), czero<C>(), czero<C>(), czero<C>()};   // rows r, r + nt, ...
+            for (int b0 = ptr[c]; b0 < ptr[c + 1]; b0 += kGhBuf) {
+                const int nb = min(kGhBuf, ptr[c + 1] - b0);
+                __syncthreads();
+                for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+                    const int k = v.cc_row[b0 + t];
+                    sk[t] = k;
+                    sv[t] = from_c128<C>(rs[k] * v.aval[v.cc_src[b0 + t]]);
                 }
-                out[r + (int64_t)c * S] = acc;
+                __syncthreads();
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int r = threadIdx.x + h * blockDim.x;
+                    if (r < S)
+                        for (int t = 0; t < nb; ++t) acc[h] = cfma(acc[h], Di[r + (int64_t)sk[t] * S], sv[t]);
+                }
             }
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                const int r = threadIdx.x + h * blockDim.x;
+                if (r < S) out[r + (int64_t)c * S] = acc[h];
+            }
+        }
     }
 }
 
@@ -582,7 +621,7 @@ int factor_levels(kore_plan *p) {
         KORE_LAUNCHED(1);
         // D_j^-1 of the odd blocks by Gauss-Jordan on [D_j | I]
         KORE_TRY((gauss_jordan<C, NB>(p, v, lv, lv.nodd, 0, ns)));
-        const int th = std::min(1024, ((S + 31) / 32) * 32);
+        const int th = std::min(512, ((S + 31) / 32) * 32);   // rows per pass (S <= 1024: two passes at most)
         if (l == 0) {
             // G_j, H_j from the sparse couplings (complex64: refined on the tensor cores),
             // then the even blocks
