@@ -94,8 +94,20 @@ def run(cmd, cwd, env=None):
     return r.stdout
 
 
-def make_case(name):
+# Pencils whose A is affine in the Rayleigh number (only the buoyancy coupling depends
+# on Ra_gap): the reference assembles A at two Rayleigh numbers; the fixture stores
+# A_a = A(Ra_a), dA = A(Ra_b) - A(Ra_a) and B (which does not depend on Ra), so that
+# A(Ra) = A_a + (Ra - Ra_a) / (Ra_b - Ra_a) dA.  Used by the critical-Rayleigh search
+# (tests/jones2000/find_Rac.py).
+RA_PAIRS = {
+    "jones2000_onset": ("jones2000_rac", 4.6e6, 4.8e6),
+}
+
+
+def make_case(name, extra=None, dst=None):
     base, overrides, profiles = CASES[name]
+    if extra:
+        overrides = dict(overrides, **extra)
     with tempfile.TemporaryDirectory(prefix=f"korefx_{name}_") as tmp:
         shutil.copytree(os.path.join(REF, "bin"), os.path.join(tmp, "bin"))
         with open(os.path.join(REF, base)) as f:
@@ -124,14 +136,46 @@ def make_case(name):
         b = np.load(os.path.join(tmp, bname))
         for k in ("data", "indices", "indptr", "shape"):
             out["B_" + k] = b[k]
+        dst = dst or os.path.join(HERE, name + ".npz")
+        np.savez_compressed(dst, **out)
+        return name, meta["sizmat"], os.path.getsize(dst)
+
+
+def make_ra_pair(name):
+    import scipy.sparse as ss
+    case, ra_a, ra_b = RA_PAIRS[name]
+    with tempfile.TemporaryDirectory(prefix=f"korefx_{name}_") as tmp:
+        za, zb = os.path.join(tmp, "a.npz"), os.path.join(tmp, "b.npz")
+        make_case(case, {"Ra_gap": repr(ra_a)}, za)
+        make_case(case, {"Ra_gap": repr(ra_b)}, zb)
+        a, b = np.load(za), np.load(zb)
+        A = [ss.csr_matrix((z["A_data"], z["A_indices"], z["A_indptr"]), shape=tuple(z["A_shape"])) for z in (a, b)]
+        Bd = [ss.csr_matrix((z["B_data"], z["B_indices"], z["B_indptr"]), shape=tuple(z["B_shape"])) for z in (a, b)]
+        if abs(Bd[0] - Bd[1]).max() != 0:
+            raise RuntimeError("B depends on Ra")
+        dA = (A[1] - A[0]).tocsr()
+        dA.eliminate_zeros()
+        meta = json.loads(str(a["meta"]))
+        meta.update(Ra_a=ra_a, Ra_b=ra_b)
+        out = {"meta": np.array(json.dumps(meta))}
+        for k, M in (("A", A[0]), ("dA", dA)):
+            M = M.tocsr()
+            out[k + "_data"], out[k + "_indices"], out[k + "_indptr"] = M.data, M.indices, M.indptr
+            out[k + "_shape"] = np.array(M.shape)
+        for k in ("data", "indices", "indptr", "shape"):
+            out["B_" + k] = a["B_" + k]
         dst = os.path.join(HERE, name + ".npz")
         np.savez_compressed(dst, **out)
         return name, meta["sizmat"], os.path.getsize(dst)
 
 
+def make_any(name):
+    return make_ra_pair(name) if name in RA_PAIRS else make_case(name)
+
+
 if __name__ == "__main__":
-    names = sys.argv[1:] or list(CASES)
+    names = sys.argv[1:] or list(CASES) + list(RA_PAIRS)
     from concurrent.futures import ProcessPoolExecutor
     with ProcessPoolExecutor(max_workers=min(4, len(names))) as ex:
-        for name, sizmat, size in ex.map(make_case, names):
+        for name, sizmat, size in ex.map(make_any, names):
             print(f"{name}: sizmat={sizmat} file={size/1e6:.2f} MB")
