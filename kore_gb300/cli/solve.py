@@ -16,6 +16,9 @@ It reads what ``bin/solve.py`` reads and writes what it writes:
 Options with no effect on this path (MUMPS/PC choices, balancing, viewers) are
 accepted and ignored with a warning; ``-kore_precision fp64|mixed`` (default mixed),
 ``-kore_seed``, ``-kore_device`` and ``-kore_refine_tol`` select this path's settings.
+``-kore_binary`` also writes the same arrays in binary form next to the text files
+(``eigenvalues0.npy``, ``{real,imag}_<field>.field.npy``): the text files of a 240k
+unknown case hold millions of numbers and take longer to write than the solve.
 """
 import os
 import sys
@@ -28,7 +31,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 KNOWN = {"st_type", "eps_nev", "eps_ncv", "eps_tol", "eps_max_it", "eps_purify", "ksp_type", "pc_type", "nbl",
-         "kore_precision", "kore_seed", "kore_device", "kore_refine_tol"}
+         "kore_precision", "kore_seed", "kore_device", "kore_refine_tol", "kore_binary"}
 IGNORED_PREFIX = ("mat_mumps", "st_pc_factor", "pc_factor", "eps_balance", "eps_true_residual", "eps_view",
                   "eps_error", "log_view", "ksp_view", "ksp_monitor", "eps_monitor", "st_ksp", "st_pc")
 
@@ -66,7 +69,7 @@ def load_csr(path):
     return ss.csr_matrix((z["data"], z["indices"], z["indptr"]), shape=tuple(z["shape"]))
 
 
-def write_fields(vec, n, par, forced):
+def write_fields(vec, n, par, forced, binary=False):
     from kore_gb300.structure import field_offsets
     off = field_offsets(n, int(par.hydro), int(par.magnetic), int(par.thermal),
                         int(getattr(par, "compositional", 0)), forced=forced)
@@ -79,6 +82,9 @@ def write_fields(vec, n, par, forced):
             np.savetxt(f, np.real(part))
         with open(f"imag_{names[key]}.field", "wb") as f:
             np.savetxt(f, np.imag(part))
+        if binary:
+            np.save(f"real_{names[key]}.field.npy", np.ascontiguousarray(np.real(part)))
+            np.save(f"imag_{names[key]}.field.npy", np.ascontiguousarray(np.imag(part)))
 
 
 def main(argv=None):
@@ -100,6 +106,7 @@ def main(argv=None):
     A = load_csr("A.npz")
     lay = layout_from_params(par)
     forced = int(getattr(par, "forcing", 0)) != 0
+    binary = bool(opts.get("kore_binary", False)) and str(opts.get("kore_binary")) != "0"
     success = 0
     if not forced:
         B = load_csr("B.npz")
@@ -131,7 +138,9 @@ def main(argv=None):
                 eigval = np.column_stack([lam.real, lam.imag])
                 with open("eigenvalues0.dat", "wb") as f:
                     np.savetxt(f, eigval)
-                write_fields(X, n, par, forced=False)
+                if binary:
+                    np.save("eigenvalues0.npy", eigval)
+                write_fields(X, n, par, forced=False, binary=binary)
                 success = nconv
             else:
                 print("No converged solution found")
@@ -154,7 +163,7 @@ def main(argv=None):
         else:
             success = 1
             print("Solution(s) computed")
-            write_fields(x, n, par, forced=True)
+            write_fields(x, n, par, forced=True, binary=binary)
     toc = timer()
     print("Solve done in", toc - tic, "seconds")
     with open("timing.dat", "ab") as f:

@@ -72,3 +72,16 @@ def test_cli_forced(gpu_lib, case, tmp_path):
     assert np.linalg.norm(x - ref) / np.linalg.norm(ref) < 1e-9
 
 
+
+
+def test_cli_binary_output_matches_text(gpu_lib, case, tmp_path):
+    """-kore_binary writes the eigenvalues and fields also as .npy, equal to the text files
+    up to the text format's 18 significant digits."""
+    meta, A, B = case("spinover")
+    write_case(str(tmp_path), meta, A, B)
+    run_cli(str(tmp_path), "-st_type", "sinvert", "-kore_precision", "fp64", "-kore_binary")
+    dat = np.loadtxt(tmp_path / "eigenvalues0.dat")
+    np.testing.assert_allclose(np.load(tmp_path / "eigenvalues0.npy"), dat, rtol=1e-17, atol=0)
+    for part in ("real", "imag"):
+        txt = np.loadtxt(tmp_path / f"{part}_flow.field")
+        np.testing.assert_allclose(np.load(tmp_path / f"{part}_flow.field.npy"), txt, rtol=1e-17, atol=0)
