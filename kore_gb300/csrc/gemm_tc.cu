@@ -7,15 +7,19 @@
 // the subtraction done by the MMA's negate-A bit.
 //
 // Data flow of one 128 x 64 tile of C = beta C + alpha (A1 B1 [+ A2 B2]):
-//   * k_tc_split writes, once per matrix, four K-major FP32 planes (Re hi, Re lo, Im hi,
-//     Im lo): A operands transposed (K contiguous per row of A), B operands as stored
-//     (column-major: K contiguous per column of B), K padded with zeros to Kp = 32 k;
+//   * k_tc_split writes, once per matrix, K-major FP32 planes: Re hi, Re lo, Im hi, Im lo
+//     of the A operands (transposed: K contiguous per row of A) and the same plus -Im hi,
+//     -Im lo of the B operands (as stored: K contiguous per column of B), K padded with
+//     zeros to Kp = 32 k;
 //   * one producer thread streams the planes of each 32-wide K slice into a two-stage
 //     shared-memory ring with cp.async.bulk.tensor (128-byte swizzle, the layout the MMA
-//     descriptors describe), each stage guarded by a "full" and an "empty" mbarrier;
-//   * one thread issues tcgen05.mma (M = 128, N = 64, K = 8 per instruction, 12 per K
-//     step) into two accumulators in tensor memory (Re: columns 0-63, Im: 64-127) and
-//     frees each stage with tcgen05.commit;
+//     descriptors describe), each stage guarded by a "full" and an "empty" mbarrier.  The
+//     B planes of a stage lie as [-Bi | Br | Bi] (hi, then lo), so the 128-row windows
+//     W1 = [Br | Bi] and W2 = [-Bi | Br] are B operands of single MMAs:
+//         [Re | Im](C) += Ar W1 + Ai W2;
+//   * one thread issues tcgen05.mma (M = 128, N = 128, K = 8 per instruction, 6 per K
+//     step: 3xTF32 of the two products) into one tensor-memory accumulator (Re: columns
+//     0-63, Im: 64-127) and frees each stage with tcgen05.commit;
 //   * the four warps read their 32 lanes (rows) back with tcgen05.ld and write C.
 // Every wait is bounded (error flag, then the kernel carries on to release its tensor
 // memory); tensor memory is allocated and freed by warp 0.
@@ -28,12 +32,18 @@
 namespace {
 
 constexpr int kTcM = 128, kTcN = 64, kTcK = 32, kTcStages = 2, kTcThreads = 128;
+constexpr int kPlanesA = 4, kPlanesB = 6;         // A: Re hi, Re lo, Im hi, Im lo; B: + -Im hi, -Im lo
 constexpr int kPlaneA = kTcM * kTcK * 4;          // 16 KB: one plane of an A slice
 constexpr int kPlaneB = kTcN * kTcK * 4;          // 8 KB
-constexpr int kStageA = 4 * kPlaneA;
-constexpr int kStageBytes = kStageA + 4 * kPlaneB;   // 96 KB
-constexpr uint32_t kTmemCols = 2 * kTcN;          // Re accumulator [0, 64), Im [64, 128)
+constexpr int kStageA = kPlanesA * kPlaneA;
+constexpr int kStageBytes = kStageA + kPlanesB * kPlaneB;   // 112 KB
+constexpr uint32_t kTmemCols = 2 * kTcN;          // [Re | Im] accumulator: columns [0, 64) and [64, 128)
 constexpr size_t kTcSmem = (size_t)kTcStages * kStageBytes + 1024 + 128;
+// Order of the B planes in a stage: [-Im hi][Re hi][Im hi][-Im lo][Re lo][Im lo]; stage
+// slot of global plane p (Re hi, Re lo, Im hi, Im lo, -Im hi, -Im lo).
+__host__ __device__ constexpr int slot_b(int p) {
+    return p == 0 ? 1 : p == 1 ? 4 : p == 2 ? 2 : p == 3 ? 5 : p == 4 ? 0 : 3;
+}
 
 struct TcJob {
     int a1, b1, a2, b2;   // matrix indices into the A and B plane sets (a2 < 0: one product)
@@ -104,11 +114,10 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
 }
 
 // Instruction descriptor of kind::tf32: D F32 (bits 4-5 = 1), A and B TF32 (bits 7-9,
-// 10-12 = 2), negate A (bit 13), both operands K-major (bits 15, 16 = 0), N >> 3 at
-// bits 17-22, M >> 4 at bits 24-28.
-__host__ __device__ constexpr uint32_t tf32_idesc(bool negate_a) {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((negate_a ? 1u : 0u) << 13) | ((uint32_t)(kTcN >> 3) << 17) |
-           ((uint32_t)(kTcM >> 4) << 24);
+// 10-12 = 2), no negation (bits 13, 14), both operands K-major (bits 15, 16 = 0),
+// N >> 3 at bits 17-22 (N = 128: the [Re | Im] window), M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t tf32_idesc() {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)((2 * kTcN) >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
 }
 
 __device__ __forceinline__ float tf32_rna(float x) {
@@ -118,9 +127,10 @@ __device__ __forceinline__ float tf32_rna(float x) {
 }
 
 // ----------------------------------------------------------------------------- split planes
-// planes[((m * 4 + p) * S + row) * Kp + k], p = Re hi, Re lo, Im hi, Im lo.
-// TRANS (A operand): row = row of X, k = column of X.  !TRANS (B operand): row = column
-// of X, k = row of X.  X is column-major S x S; k in [S, Kp) is zero.
+// planes[((m * P + p) * S + row) * Kp + k], p = Re hi, Re lo, Im hi, Im lo (P = 4, A
+// operands) and -Im hi, -Im lo (P = 6, B operands).  TRANS (A operand): row = row of X,
+// k = column of X.  !TRANS (B operand): row = column of X, k = row of X.  X is
+// column-major S x S; k in [S, Kp) is zero.
 template <bool TRANS>
 __global__ void __launch_bounds__(256) k_tc_split(const float2 *const *__restrict__ src, int S, int Kp,
                                                   float *__restrict__ planes) {
@@ -130,7 +140,7 @@ __global__ void __launch_bounds__(256) k_tc_split(const float2 *const *__restric
     const int k0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
     const int64_t plane = (int64_t)S * Kp;
-    float *base = planes + (int64_t)m * 4 * plane;
+    float *base = planes + (int64_t)m * (TRANS ? kPlanesA : kPlanesB) * plane;
     auto put = [&](int row, int k, float2 v) {
         const float rh = tf32_rna(v.x), ih = tf32_rna(v.y);
         const int64_t o = (int64_t)row * Kp + k;
@@ -138,6 +148,10 @@ __global__ void __launch_bounds__(256) k_tc_split(const float2 *const *__restric
         base[plane + o] = v.x - rh;
         base[2 * plane + o] = ih;
         base[3 * plane + o] = v.y - ih;
+        if (!TRANS) {
+            base[4 * plane + o] = -ih;
+            base[5 * plane + o] = -(v.y - ih);
+        }
     };
     if (TRANS) {
         // read X(r0 + tx, k0 + j) along its rows, write row r0 + j along k
@@ -198,18 +212,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const __grid_constant
                 const int ia = pair ? job.a2 : job.a1, ib = pair ? job.b2 : job.b1;
                 unsigned char *sa = smem + (size_t)s * kStageBytes, *sb = sa + kStageA;
 #pragma unroll
-                for (int p = 0; p < 4; ++p) {
-                    tma_load_3d(sa + p * kPlaneA, &P.amap, &full[s], kq * kTcK, tm * kTcM, ia * 4 + p);
-                    tma_load_3d(sb + p * kPlaneB, &P.bmap, &full[s], kq * kTcK, tn * kTcN, ib * 4 + p);
-                }
+                for (int p = 0; p < kPlanesA; ++p)
+                    tma_load_3d(sa + p * kPlaneA, &P.amap, &full[s], kq * kTcK, tm * kTcM, ia * kPlanesA + p);
+#pragma unroll
+                for (int p = 0; p < kPlanesB; ++p)
+                    tma_load_3d(sb + slot_b(p) * kPlaneB, &P.bmap, &full[s], kq * kTcK, tn * kTcN, ib * kPlanesB + p);
             }
         }
         __syncwarp();
     } else if (warp == 1) {
         if (lane == 0) {
             // MMA issuer
-            const uint32_t ip = tf32_idesc(false), in = tf32_idesc(true);
-            const uint32_t dr = tmem, di = tmem + (uint32_t)kTcN;
+            const uint32_t id = tf32_idesc();
             for (int ks = 0; ks < nstage; ++ks) {
                 const int s = ks % kTcStages;
                 const uint32_t ph = (uint32_t)(ks / kTcStages) & 1u;
@@ -218,27 +232,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_gemm(const __grid_constant
                 const uint32_t sa = smem_u32(smem + (size_t)s * kStageBytes), sb = sa + kStageA;
 #pragma unroll
                 for (int k8 = 0; k8 < kTcK / 8; ++k8) {
-                    uint64_t a[4], b[4];
+                    uint64_t a[kPlanesA];
 #pragma unroll
-                    for (int p = 0; p < 4; ++p) {
-                        a[p] = sw128_desc(sa + p * kPlaneA) + (uint64_t)(2 * k8);   // + 32 bytes of K
-                        b[p] = sw128_desc(sb + p * kPlaneB) + (uint64_t)(2 * k8);
-                    }
+                    for (int p = 0; p < kPlanesA; ++p) a[p] = sw128_desc(sa + p * kPlaneA) + (uint64_t)(2 * k8);
+                    // 128-row windows of the B planes (+ 32 bytes of K per step of 8)
+                    const uint64_t w1h = sw128_desc(sb + 1 * kPlaneB) + (uint64_t)(2 * k8);   // [Br hi | Bi hi]
+                    const uint64_t w2h = sw128_desc(sb + 0 * kPlaneB) + (uint64_t)(2 * k8);   // [-Bi hi | Br hi]
+                    const uint64_t w1l = sw128_desc(sb + 4 * kPlaneB) + (uint64_t)(2 * k8);   // [Br lo | Bi lo]
+                    const uint64_t w2l = sw128_desc(sb + 3 * kPlaneB) + (uint64_t)(2 * k8);   // [-Bi lo | Br lo]
                     const uint32_t acc = (ks == 0 && k8 == 0) ? 0u : 1u;
-                    // Re += Ar Br - Ai Bi
-                    tc_mma(dr, a[0], b[0], ip, acc);
-                    tc_mma(dr, a[0], b[1], ip, 1u);
-                    tc_mma(dr, a[1], b[0], ip, 1u);
-                    tc_mma(dr, a[2], b[2], in, 1u);
-                    tc_mma(dr, a[2], b[3], in, 1u);
-                    tc_mma(dr, a[3], b[2], in, 1u);
-                    // Im += Ar Bi + Ai Br
-                    tc_mma(di, a[0], b[2], ip, acc);
-                    tc_mma(di, a[0], b[3], ip, 1u);
-                    tc_mma(di, a[1], b[2], ip, 1u);
-                    tc_mma(di, a[2], b[0], ip, 1u);
-                    tc_mma(di, a[2], b[1], ip, 1u);
-                    tc_mma(di, a[3], b[0], ip, 1u);
+                    // [Re | Im] += Ar [Br | Bi]
+                    tc_mma(tmem, a[0], w1h, id, acc);
+                    tc_mma(tmem, a[0], w1l, id, 1u);
+                    tc_mma(tmem, a[1], w1h, id, 1u);
+                    // [Re | Im] += Ai [-Bi | Br]
+                    tc_mma(tmem, a[2], w2h, id, 1u);
+                    tc_mma(tmem, a[2], w2l, id, 1u);
+                    tc_mma(tmem, a[3], w2h, id, 1u);
                 }
                 tc_commit(&empty[s]);   // the slot is free once these MMAs have read it
             }
@@ -290,14 +300,14 @@ int tc_run(cudaStream_t st, int device, int S, const float2 *const *srcA, int nA
     if (njobs == 0) return KORE_OK;
     if (nA > 65535 || nB > 65535) return KORE_EINVAL;
     const int Kp = tc_kp(S);
-    float *pa = planes, *pb = planes + (int64_t)nA * 4 * S * Kp;
+    float *pa = planes, *pb = planes + (int64_t)nA * kPlanesA * S * Kp;
     const dim3 sg(Kp / 32, kore_div_up(S, 32));
     k_tc_split<true><<<dim3(sg.x, sg.y, nA), dim3(32, 8), 0, st>>>(srcA, S, Kp, pa);
     k_tc_split<false><<<dim3(sg.x, sg.y, nB), dim3(32, 8), 0, st>>>(srcB, S, Kp, pb);
     KORE_LAUNCHED(2);
     TcParams P;
-    const uint64_t da[3] = {(uint64_t)Kp, (uint64_t)S, (uint64_t)4 * nA};
-    const uint64_t db[3] = {(uint64_t)Kp, (uint64_t)S, (uint64_t)4 * nB};
+    const uint64_t da[3] = {(uint64_t)Kp, (uint64_t)S, (uint64_t)kPlanesA * nA};
+    const uint64_t db[3] = {(uint64_t)Kp, (uint64_t)S, (uint64_t)kPlanesB * nB};
     const uint64_t sd[2] = {(uint64_t)Kp * 4, (uint64_t)S * Kp * 4};
     const uint32_t ba[3] = {kTcK, kTcM, 1}, bb[3] = {kTcK, kTcN, 1};
     KORE_TRY(kore_encode_f32_3d(&P.amap, pa, da, sd, ba, 1));
@@ -370,9 +380,12 @@ void kore_tc_level_bytes(const kore_plan *p, int cap, int64_t *plane_bytes, int6
         const int64_t ne = p->lev[l].neven, no = p->lev[l].nodd;
         // even update (levels >= 1): 2 neven A + 2 nodd B matrices, 3 neven jobs;
         // G, H and their refinement (every level): nodd A + 2 nodd B matrices, 2 nodd jobs
+        // planes: 4 per A and 6 per B matrix
+        const int64_t np_ = std::max(l > 0 ? 2 * ne * kPlanesA + 2 * no * kPlanesB : 0,
+                                     no * kPlanesA + 2 * no * kPlanesB) * cap;
         const int64_t nm = std::max(l > 0 ? 2 * (ne + no) : 0, 3 * no) * cap;
         const int64_t nj = std::max(l > 0 ? 3 * ne : 0, 2 * no) * cap;
-        pl = std::max(pl, nm * 4 * S * Kp * 4);
+        pl = std::max(pl, np_ * S * Kp * 4);
         tb = std::max(tb, nm * 8 + nj * (int64_t)sizeof(TcJob) + 64);
     }
     *plane_bytes = pl;
@@ -556,7 +569,7 @@ extern "C" int kore_tc_selftest(int device, int S, int nmat, double *max_rel_err
     ck(cudaMalloc(&B, nmat * SS * sizeof(float2)));
     ck(cudaMalloc(&C, nmat * SS * sizeof(float2)));
     ck(cudaMalloc(&C0, nmat * SS * sizeof(float2)));
-    ck(cudaMalloc(&planes, (size_t)2 * nmat * 4 * S * Kp * sizeof(float)));
+    ck(cudaMalloc(&planes, (size_t)nmat * (kPlanesA + kPlanesB) * S * Kp * sizeof(float)));
     ck(cudaMalloc(&tab, (size_t)2 * nmat * 8 + (size_t)nmat * sizeof(TcJob)));
     ck(cudaMalloc(&err, sizeof(double)));
     ck(cudaMalloc(&flag, sizeof(int)));

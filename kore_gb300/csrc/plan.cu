@@ -535,10 +535,10 @@ int kore_plan_estimate_bytes(const kore_pencil_desc *d, int precision, int nshif
         int64_t nm = 0, nj = 0;
         for (int64_t l = 0; l < nlev; ++l) {
             const int64_t ne = Ks[l] - Ks[l] / 2, no = Ks[l] / 2;
-            nm = std::max<int64_t>(nm, std::max<int64_t>(l > 0 ? 2 * Ks[l] : 0, 3 * no));
+            nm = std::max<int64_t>(nm, std::max<int64_t>(l > 0 ? 4 * ne + 6 * no : 0, 4 * no + 6 * no) * 2);
             nj = std::max<int64_t>(nj, std::max<int64_t>(l > 0 ? 3 * ne : 0, 2 * no));
         }
-        b += c * (nm * 4 * S * Kp * 4 + nm * 8 + nj * 32 + 64);
+        b += c * (nm / 2 * S * Kp * 4 + nm * 8 + nj * 32 + 64);   // nm / 2 planes of S x Kp floats
     }
     b += c * (3 * np * 16 + 2 * (np / 64 + np / 8 + 1024) * 8 + (3 * nlev + 1) * K * 4 + ell * e + 128);
     b += 2 * d->n * c * 16;   // kore_solve's device copies of b and x
