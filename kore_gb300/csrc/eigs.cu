@@ -71,6 +71,12 @@ __device__ inline double2 csqrt_(double2 z) {
 
 __device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
 
+__device__ __forceinline__ double2 shfl_xor_c(double2 v, int o) {
+    v.x = __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y = __shfl_xor_sync(0xffffffffu, v.y, o);
+    return v;
+}
+
 // G = [c s; -conj(s) c] with G [x; y] = [r; 0]; c = |x| / n, s = (x / |x|) conj(y) / n,
 // n = sqrt(|x|^2 + |y|^2), evaluated with two reciprocal square roots.
 __device__ __forceinline__ void givens_r(double2 x, double2 y, double &c, double2 &s) {
@@ -108,35 +114,28 @@ __device__ __forceinline__ void apply_rot(double2 *H, double2 *Q, int m, int k, 
     const int nlow = (r1 > k + 2) ? 1 : 0;             // row k+2 of columns k, k+1
     const int nleft = (c0 < k) ? 1 : 0;                // column k-1 of rows k, k+1
     const int total = nrow + ncol + nlow + nleft + m;
+    // Every item is a pair (a, b) of one matrix: rows k, k+1 of a column (G from the left,
+    // u = s) or columns k, k+1 of a row (G^H from the right, u = conj(s)); both are
+    // a' = c a + u b, b' = c b - conj(u) a.  Only the addressing differs between items,
+    // so the FP64 arithmetic runs once per warp instead of once per divergent branch.
     for (int t = tid; t < total; t += nt) {
-        int u = t;
+        int u = t, ia, step;
+        bool left;
+        double2 *M = H;
         if (u < nrow) {
-            const int j = k + 2 + u;
-            const double2 a = H[k + j * m], b = H[k + 1 + j * m];
-            H[k + j * m] = c * a + s * b;
-            H[k + 1 + j * m] = c * b - conjg(s) * a;
-            continue;
+            ia = k + (k + 2 + u) * m; step = 1; left = true;
+        } else if ((u -= nrow) < ncol + nlow) {
+            ia = ((u < ncol) ? u : k + 2) + k * m; step = m; left = false;
+        } else if ((u -= ncol + nlow) < nleft) {
+            ia = k + (k - 1) * m; step = 1; left = true;
+        } else {
+            u -= nleft;
+            M = Q; ia = u + k * m; step = m; left = false;
         }
-        u -= nrow;
-        if (u < ncol + nlow) {
-            const int i = (u < ncol) ? u : k + 2;
-            const double2 a = H[i + k * m], b = H[i + (k + 1) * m];
-            H[i + k * m] = c * a + b * conjg(s);
-            H[i + (k + 1) * m] = c * b - a * s;
-            continue;
-        }
-        u -= ncol + nlow;
-        if (u < nleft) {
-            const int j = k - 1;
-            const double2 a = H[k + j * m], b = H[k + 1 + j * m];
-            H[k + j * m] = c * a + s * b;
-            H[k + 1 + j * m] = c * b - conjg(s) * a;
-            continue;
-        }
-        u -= nleft;
-        const double2 a = Q[u + k * m], b = Q[u + (k + 1) * m];
-        Q[u + k * m] = c * a + b * conjg(s);
-        Q[u + (k + 1) * m] = c * b - a * s;
+        const double2 a = M[ia], b = M[ia + step];
+        const double2 us = left ? s : conjg(s);
+        M[ia] = c * a + us * b;
+        M[ia + step] = c * b - conjg(us) * a;
     }
 }
 
@@ -185,22 +184,35 @@ __global__ void __launch_bounds__(kSchurT) k_schur(const double2 *__restrict__ H
             vsh[i] = vinv * v;
         }
         __syncthreads();
-        // H <- (I - 2 v v^H) H (rows k+1.., columns k..), one column per thread
-        for (int c = k + tid; c < m; c += kSchurT) {
+        // H <- (I - 2 v v^H) H (rows k+1.., columns k..): four lanes per column, each
+        // summing every fourth row, so the dependent FP64 chain is len / 4 long
+        for (int base = 0; base < 4 * (m - k); base += kSchurT) {
+            const int c = k + (base + tid) / 4, sub = tid & 3;
+            const bool on = c < m;
             double2 t = mk(0.0, 0.0);
-            for (int i = 0; i < len; ++i) t = cfmaconj(t, vsh[i], H[k + 1 + i + c * m]);
+            if (on)
+                for (int i = sub; i < len; i += 4) t = cfmaconj(t, vsh[i], H[k + 1 + i + c * m]);
+            t = t + shfl_xor_c(t, 1);
+            t = t + shfl_xor_c(t, 2);
             t = 2.0 * t;
-            for (int i = 0; i < len; ++i) H[k + 1 + i + c * m] = cfms(H[k + 1 + i + c * m], vsh[i], t);
+            if (on)
+                for (int i = sub; i < len; i += 4) H[k + 1 + i + c * m] = cfms(H[k + 1 + i + c * m], vsh[i], t);
         }
         __syncthreads();
-        // H <- H (I - 2 v v^H), Q <- Q (I - 2 v v^H): one row per thread
-        for (int r = tid; r < 2 * m; r += kSchurT) {
+        // H <- H (I - 2 v v^H), Q <- Q (I - 2 v v^H): two lanes per row
+        for (int base = 0; base < 4 * m; base += kSchurT) {
+            const int r = (base + tid) / 2, sub = tid & 1;
+            const bool on = r < 2 * m;
             double2 *M = (r < m) ? H : Q;
             const int rr = (r < m) ? r : r - m;
             double2 t = mk(0.0, 0.0);
-            for (int i = 0; i < len; ++i) t = cfma(t, M[rr + (k + 1 + i) * m], vsh[i]);
+            if (on)
+                for (int i = sub; i < len; i += 2) t = cfma(t, M[rr + (k + 1 + i) * m], vsh[i]);
+            t = t + shfl_xor_c(t, 1);
             t = 2.0 * t;
-            for (int i = 0; i < len; ++i) M[rr + (k + 1 + i) * m] = cfms(M[rr + (k + 1 + i) * m], t, conjg(vsh[i]));
+            if (on)
+                for (int i = sub; i < len; i += 2)
+                    M[rr + (k + 1 + i) * m] = cfms(M[rr + (k + 1 + i) * m], t, conjg(vsh[i]));
         }
         __syncthreads();
         for (int i = 2 + tid; i < len + 1; i += kSchurT) H[k + i + k * m] = mk(0.0, 0.0);
@@ -210,14 +222,20 @@ __global__ void __launch_bounds__(kSchurT) k_schur(const double2 *__restrict__ H
     // --- shifted QR sweeps (complete Schur form, transformations accumulated in Q)
     const double eps = 2.220446049250313e-16;
     int hi = m - 1, iter = 0, total = 0, fail = 0;
+    __shared__ int lred[kSchurT / 32];
     while (hi > 0) {
-        int l = hi;
-        while (l > 0) {
-            double ref = cabs1(H[l - 1 + (l - 1) * m]) + cabs1(H[l + l * m]);
+        // l = the largest index in [1, hi] whose subdiagonal entry is negligible, else 0:
+        // one thread per candidate, maximum over the CTA
+        int l = 0;
+        for (int q = tid + 1; q <= hi; q += kSchurT) {
+            double ref = cabs1(H[q - 1 + (q - 1) * m]) + cabs1(H[q + q * m]);
             if (ref == 0.0) ref = 1.0;
-            if (cabs1(H[l + (l - 1) * m]) <= eps * ref) break;
-            --l;
+            if (cabs1(H[q + (q - 1) * m]) <= eps * ref) l = q;
         }
+        l = __reduce_max_sync(0xffffffffu, l);
+        if (lane == 0) lred[wid] = l;
+        __syncthreads();
+        for (int wv = 0; wv < kSchurT / 32; ++wv) l = max(l, lred[wv]);
         __syncthreads();
         if (l > 0 && tid == 0) H[l + (l - 1) * m] = mk(0.0, 0.0);
         __syncthreads();
@@ -320,13 +338,18 @@ __global__ void __launch_bounds__(kSchurT) k_schur(const double2 *__restrict__ H
 }
 
 // ----------------------------------------------------------------------------- tall-skinny kernels
-// partial[b*ncol + c] = sum over the CTA's rows of conj(V[:,c]) w, c < ncol
+// partial[b*nc + c] = sum over the CTA's rows of conj(V[:,c]) w for c < ncol, and, with
+// with_norm, entry c = ncol = sum |w|^2 (nc = ncol + with_norm).  run (may be null):
+// the kernel returns at once unless *run != 0.
 constexpr int kDotThreads = 256;
 constexpr int kDotChunk = 8;
 __global__ void __launch_bounds__(kDotThreads) k_mdot(int64_t np, int ncol, const double2 *__restrict__ V,
-                                                      const double2 *__restrict__ w, double2 *__restrict__ partial) {
+                                                      const double2 *__restrict__ w, double2 *__restrict__ partial,
+                                                      int with_norm, const int *__restrict__ run) {
+    if (run && *run == 0) return;
     __shared__ double2 sm[kDotThreads / 32][kDotChunk];
-    for (int c0 = 0; c0 < ncol; c0 += kDotChunk) {
+    const int nc = ncol + with_norm;
+    for (int c0 = 0; c0 < nc; c0 += kDotChunk) {
         double2 acc[kDotChunk];
 #pragma unroll
         for (int t = 0; t < kDotChunk; ++t) acc[t] = mk(0.0, 0.0);
@@ -334,7 +357,7 @@ __global__ void __launch_bounds__(kDotThreads) k_mdot(int64_t np, int ncol, cons
             const double2 wr = w[r];
 #pragma unroll
             for (int t = 0; t < kDotChunk; ++t)
-                if (c0 + t < ncol) acc[t] = cfmaconj(acc[t], V[r + (int64_t)(c0 + t) * np], wr);
+                if (c0 + t < nc) acc[t] = cfmaconj(acc[t], (c0 + t < ncol) ? V[r + (int64_t)(c0 + t) * np] : wr, wr);
         }
 #pragma unroll
         for (int t = 0; t < kDotChunk; ++t) {
@@ -342,18 +365,19 @@ __global__ void __launch_bounds__(kDotThreads) k_mdot(int64_t np, int ncol, cons
             if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5][t] = v;
         }
         __syncthreads();
-        if (threadIdx.x < kDotChunk && c0 + (int)threadIdx.x < ncol) {
+        if (threadIdx.x < kDotChunk && c0 + (int)threadIdx.x < nc) {
             double2 s = mk(0.0, 0.0);
             for (int wv = 0; wv < kDotThreads / 32; ++wv) s = s + sm[wv][threadIdx.x];
-            partial[blockIdx.x * (int64_t)ncol + c0 + threadIdx.x] = s;
+            partial[blockIdx.x * (int64_t)nc + c0 + threadIdx.x] = s;
         }
         __syncthreads();
     }
 }
 
-// h[c] (+)= sum_b partial[b*ncol + c]; also writes into Hbar column `col` (accumulate)
+// h[c] (+)= sum_b partial[b*ncol + c] (one CTA per c); returns at once unless *run != 0
 __global__ void k_mdot_reduce(int nblk, int ncol, const double2 *__restrict__ partial, double2 *__restrict__ h,
-                              int accumulate) {
+                              int accumulate, const int *__restrict__ run) {
+    if (run && *run == 0) return;
     const int c = blockIdx.x;
     double2 s = mk(0.0, 0.0);
     for (int b = threadIdx.x; b < nblk; b += blockDim.x) s = s + partial[(int64_t)b * ncol + c];
@@ -368,9 +392,10 @@ __global__ void k_mdot_reduce(int nblk, int ncol, const double2 *__restrict__ pa
     }
 }
 
-// w -= V h  (ncol columns); h_cur is this pass's coefficients
+// w -= V h  (ncol columns); h is this pass's coefficients; returns at once unless *run != 0
 __global__ void k_mgs_update(int64_t np, int ncol, const double2 *__restrict__ V, const double2 *__restrict__ h,
-                             double2 *__restrict__ w) {
+                             double2 *__restrict__ w, const int *__restrict__ run) {
+    if (run && *run == 0) return;
     __shared__ double2 hs[kMaxNcv + 1];
     for (int c = threadIdx.x; c < ncol; c += blockDim.x) hs[c] = h[c];
     __syncthreads();
@@ -396,6 +421,29 @@ __global__ void k_nrm2_partial(int64_t np, const double2 *__restrict__ w, double
         partial[blockIdx.x] = t;
     }
 }
+// Refinement decision of classical Gram-Schmidt (SLEPc's default, refinement "if needed"
+// with eta = 1/sqrt(2)): h1[ncol].x = ||w||^2 before the first pass; the norm after it
+// is sqrt(||w||^2 - sum |h1_c|^2) (exact for orthonormal V); a second pass runs when
+// that is below eta ||w||.  Clears h2, which a skipped second pass leaves untouched.
+__global__ void k_refine_decide(const double2 *__restrict__ h1, int ncol, double2 *__restrict__ h2,
+                                int *__restrict__ run2) {
+    __shared__ double sm[32];
+    double s = 0.0;
+    for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
+        s += abs2(h1[c]);
+        h2[c] = mk(0.0, 0.0);
+    }
+    s = warp_sum_d(s);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int wv = 0; wv < (int)(blockDim.x >> 5); ++wv) t += sm[wv];
+        const double onrm2 = h1[ncol].x;
+        *run2 = (onrm2 - t < 0.5 * onrm2) ? 1 : 0;
+    }
+}
+
 // beta = sqrt(sum partial); Hbar[j+1 + j*ld] = beta; h (ncol entries) copied into Hbar column j
 __global__ void k_finish_col(int nblk, const double *__restrict__ partial, const double2 *__restrict__ h, int ncol,
                              double2 *__restrict__ Hbar, int ld, int j, double *__restrict__ beta_out) {
@@ -475,6 +523,7 @@ struct Ctx {
     double2 *V, *Vtmp, *w, *t1;
     double2 *Hbar, *partial, *h;
     double *dpart, *beta;
+    int *run2;          // second Gram-Schmidt pass needed (device flag)
     double refine_tol;
 };
 
@@ -507,14 +556,19 @@ int apply_op(Ctx &c, const double2 *v, double2 *out) {
 int orthonormalise(Ctx &c, int ncol, int j, int ldh) {
     kore_plan *p = c.p;
     if (p->prof) KORE_TRY(kore_prof_mark(p, 3, true));
-    for (int pass = 0; pass < 2; ++pass) {
-        k_mdot<<<c.grid, kDotThreads, 0, p->stream>>>(c.np, ncol, c.V, c.w, c.partial);
-        k_mdot_reduce<<<ncol, 256, 0, p->stream>>>((int)c.grid, ncol, c.partial, c.h + (pass ? kMaxNcv + 1 : 0), 0);
-        k_mgs_update<<<c.grid, 256, 0, p->stream>>>(c.np, ncol, c.V, c.h + (pass ? kMaxNcv + 1 : 0), c.w);
-        KORE_LAUNCHED(3);
-    }
+    // first pass, with ||w||^2 as entry ncol of h1
+    double2 *h1 = c.h, *h2 = c.h + kMaxNcv + 1;
+    k_mdot<<<c.grid, kDotThreads, 0, p->stream>>>(c.np, ncol, c.V, c.w, c.partial, 1, nullptr);
+    k_mdot_reduce<<<ncol + 1, 256, 0, p->stream>>>((int)c.grid, ncol + 1, c.partial, h1, 0, nullptr);
+    k_mgs_update<<<c.grid, 256, 0, p->stream>>>(c.np, ncol, c.V, h1, c.w, nullptr);
+    k_refine_decide<<<1, 256, 0, p->stream>>>(h1, ncol, h2, c.run2);
+    // second pass if needed
+    k_mdot<<<c.grid, kDotThreads, 0, p->stream>>>(c.np, ncol, c.V, c.w, c.partial, 0, c.run2);
+    k_mdot_reduce<<<ncol, 256, 0, p->stream>>>((int)c.grid, ncol, c.partial, h2, 0, c.run2);
+    k_mgs_update<<<c.grid, 256, 0, p->stream>>>(c.np, ncol, c.V, h2, c.w, c.run2);
+    KORE_LAUNCHED(7);
     // h = h1 + h2
-    k_mdot_reduce<<<ncol, 32, 0, p->stream>>>(1, ncol, c.h + kMaxNcv + 1, c.h, 1);
+    k_mdot_reduce<<<ncol, 32, 0, p->stream>>>(1, ncol, h2, h1, 1, nullptr);
     k_nrm2_partial<<<c.grid, 256, 0, p->stream>>>(c.np, c.w, c.dpart);
     k_finish_col<<<1, 256, 0, p->stream>>>((int)c.grid, c.dpart, c.h, ncol, c.Hbar, ldh, j, c.beta);
     k_scale_copy<<<c.grid, 256, 0, p->stream>>>(c.np, c.w, c.beta, c.V + (int64_t)(j + 1) * c.np);
@@ -569,6 +623,7 @@ int kore_eigs_impl(kore_plan *p, const kore_eps_opts *o, double *evals, double *
     c.dpart = reinterpret_cast<double *>(c.partial + 2048 * (kMaxNcv + 1));
     c.beta = c.dpart + 2048;
     int *dinfo = reinterpret_cast<int *>(c.beta + 8);
+    c.run2 = dinfo + 4;
     if (c.grid > 2048) return KORE_EINVAL;
 
     // start vector

@@ -55,7 +55,7 @@ struct FV {
     C *Dinv, *G, *H, *Dw, *LU, *T;
     int *piv, *pidx, *used, *err;
     const int *cc_ptr, *cc_row, *cc_src;
-    const int *ell_col;      // level-0 coupling rows of the even blocks (kore_plan::d_ell_*)
+    const int *ell_col;      // level-0 coupling rows of every block (kore_plan::d_ell_*)
     const C *ell_val;
     int ell_w;
     int64_t ell_stride;
@@ -129,9 +129,9 @@ __global__ void k_ell_fill(int64_t ell_stride, int ell_w, int ntile, int S, int6
         const int e = src[idx];
         C v = czero<C>();
         if (e >= 0) {
-            const int64_t lane = idx & 31, tile = idx / 32 / ell_w;   // tile = bi * ntile + t
+            const int64_t lane = idx & 31, tile = idx / 32 / ell_w;   // tile = block * ntile + t
             const int64_t bi = tile / ntile, t = tile - bi * ntile;
-            const int64_t row = 2 * bi * S + t * 32 + lane;
+            const int64_t row = bi * S + t * 32 + lane;
             v = from_c128<C>(rscale[s * np + row] * aval[e]);
         }
         val[s * ell_stride + idx] = v;
@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(512) k_even_l0(FV<C> v, BcrLevel lv) {
         C dsum[kEvenCW], lsum[kEvenCW], usum[kEvenCW];
 #pragma unroll
         for (int t = 0; t < kEvenCW; ++t) dsum[t] = lsum[t] = usum[t] = czero<C>();
-        const int64_t ebase = ((e * ntile + r / 32) * (int64_t)v.ell_w) * 32 + (r & 31);
+        const int64_t ebase = ((q * ntile + r / 32) * (int64_t)v.ell_w) * 32 + (r & 31);
         for (int k = 0; k < v.ell_w; ++k) {
             const int col = v.ell_col[ebase + (int64_t)k * 32];
             if (col < 0) continue;
@@ -751,7 +751,7 @@ int ensure_factor_storage(kore_plan *p, int cap, size_t elt) {
     // per-CTA maxima of the residual products: (np / 64 + np / 8 + 2) CTAs at most, 2 each
     KORE_TRY(kore_alloc(p, (void **)&p->d_part, c * 2 * (size_t)(p->np / 64 + p->np / 8 + 1024) * sizeof(double)));
     KORE_TRY(kore_alloc(p, (void **)&p->d_ir, c * sizeof(IrState)));
-    KORE_TRY(kore_alloc(p, (void **)&p->d_cnt, c * (size_t)(3 * p->nlev + 1) * p->K * sizeof(int)));
+    KORE_TRY(kore_alloc(p, (void **)&p->d_cnt, c * (size_t)p->sweep_stages() * p->K * sizeof(int)));
     KORE_TRY(kore_alloc(p, &p->d_ell_val, c * std::max<int64_t>(p->ell_stride(), 1) * elt));
     if (elt == sizeof(float2)) {
         int64_t pl = 0, tb = 0;

@@ -95,11 +95,13 @@ struct kore_plan {
     int *d_piv = nullptr;             // nodd_max x S per shift: pivot row chosen for column k
     int *d_pidx = nullptr;            // nodd_max x S per shift: position of a row in the current panel or -1
     int *d_used = nullptr;            // nodd_max x S per shift: row already used as a pivot
-    // Level-0 couplings of the even blocks (the rows that the first reduction updates
-    // from the CSR) as padded rows, tile by tile: entry k of row r of tile (bi, t) at
-    // ((bi * ntile + t) * ell_w + k) * 32 + r % 32, ntile = ceil(S / 32).
+    // Level-0 couplings (the entries of a block's rows in the columns of its two
+    // neighbours) as padded rows, tile by tile: entry k of row r of tile t of block i at
+    // ((i * ntile + t) * ell_w + k) * 32 + r % 32, ntile = ceil(S / 32).  The first
+    // reduction updates the even blocks' right-hand sides from them, and the last stage
+    // of the back substitution forms the odd blocks' right-hand sides from them.
     int ell_w = 0;                    // padded width (multiple of 8) of a coupling row
-    int64_t ell_rows = 0;             // even blocks of level 0 x ntile x 32
+    int64_t ell_rows = 0;             // K x ntile x 32
     int64_t ell_nnz = 0;              // coupling entries (without the padding)
     // Level-0 couplings of the odd blocks j (rows of block j, columns of block j-1 for
     // side 0 and of block j+1 for side 1) by column, for G_j = D_j^-1 L_j and
@@ -120,6 +122,8 @@ struct kore_plan {
     int64_t t_stride() const { return (int64_t)nodd_max * 2 * S * S; }
     int64_t p_stride() const { return (int64_t)nodd_max * S; }
     int64_t ell_stride() const { return ell_rows * ell_w; }
+    // stages of one sweep: A_l, B_l (l < nlev), the top block, C_l (nlev > l >= 1), E_0, C_0
+    int sweep_stages() const { return nlev > 0 ? 3 * nlev + 2 : 1; }
 
     // solve workspace (padded, complex128 unless noted)
     double2 *d_v[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -133,7 +137,7 @@ struct kore_plan {
     double *h_red = nullptr;          // pinned host mirror
     int *d_err = nullptr;
     unsigned *d_bar = nullptr;
-    int *d_cnt = nullptr;             // sweep completion counters (shift_cap x (3 nlev + 1) x K)
+    int *d_cnt = nullptr;             // sweep completion counters (shift_cap x sweep_stages() x K)
     IrState *d_ir = nullptr;          // one per shift
 
     // Krylov-Schur workspace

@@ -162,19 +162,19 @@ int permute_csr(const kore_plan *p, const std::vector<int64_t> &orig2slot, const
 int build_ell(kore_plan *p, const std::vector<int> &row, const std::vector<int> &col, const std::vector<int> &split) {
     const int64_t S = p->S;
     const int nt = (int)((S + 31) / 32);
-    const int64_t ne = p->nlev > 0 ? p->lev[0].neven : 0;
+    const int64_t nb = p->nlev > 0 ? p->K : 0;
     int w = 1;
-    for (int64_t bi = 0; bi < ne; ++bi)
+    for (int64_t bi = 0; bi < nb; ++bi)
         for (int64_t r = 0; r < S; ++r) {
-            const int64_t q = 2 * bi * S + r;
+            const int64_t q = bi * S + r;
             w = std::max(w, (split[2 * q] - row[q]) + (row[q + 1] - split[2 * q + 1]));
         }
     p->ell_w = (w + 7) & ~7;
-    p->ell_rows = ne * nt * 32;
+    p->ell_rows = nb * nt * 32;
     std::vector<int> ecol(std::max<int64_t>(p->ell_stride(), 1), -1), esrc(ecol.size(), -1);
-    for (int64_t bi = 0; bi < ne; ++bi)
+    for (int64_t bi = 0; bi < nb; ++bi)
         for (int64_t r = 0; r < S; ++r) {
-            const int64_t q = 2 * bi * S + r;
+            const int64_t q = bi * S + r;
             const int64_t base = ((bi * nt + r / 32) * p->ell_w) * 32 + r % 32;
             int k = 0;
             auto put = [&](int e) {
@@ -457,14 +457,18 @@ int kore_profile(kore_plan *p, int enable, double *out) {
         out[1] = (double)(irs.sweeps_total - p->sweeps_at_enable);
         out[2] = p->prof_ms[1];
         out[3] = (double)p->prof_n[1];
-        // one sweep reads every D^-1, G, H block once, the dense couplings of the even
-        // blocks of levels >= 1, the level-0 couplings of the even blocks (a value in
-        // factor precision + a 4 B index per entry), the right-hand side (16 B) and row
-        // scales (8 B) and writes x (16 B); the reduction vectors f, z, x in factor
-        // precision are read and written about twice each
-        double lu = 0.0;
-        for (int l = 1; l < p->nlev; ++l) lu += 2.0 * p->lev[l].neven;
-        out[4] = (3.0 * K + lu) * S * S * e + (double)p->ell_nnz * (e + 4.0) + np * (16.0 + 8.0 + 16.0) +
+        // one sweep reads the D^-1, G, H blocks of the odd blocks of levels >= 1 and the
+        // top block once, D^-1 of the level-0 odd blocks twice (no G, H at level 0), the
+        // dense couplings of the even blocks of levels >= 1, the level-0 coupling rows of
+        // every block (a value in factor precision + a 4 B index per entry), the
+        // right-hand side (16 B) and row scales (8 B) and writes x (16 B); the reduction
+        // vectors f, z, x in factor precision are read and written about twice each
+        double lu = 0.0, mats = 1.0;
+        for (int l = 0; l < p->nlev; ++l) {
+            mats += (l == 0 ? 2.0 : 3.0) * p->lev[l].nodd;
+            if (l > 0) lu += 2.0 * p->lev[l].neven;
+        }
+        out[4] = (mats + lu) * S * S * e + (double)p->ell_nnz * (e + 4.0) + np * (16.0 + 8.0 + 16.0) +
                  6.0 * np * e;
         // Gauss-Jordan on [D_j | L_j | U_j | I] for every eliminated block (trailing update
         // 8 S nb (4S - k0 - nb) real flops per panel, ~28 S^3 per block) and four dense
@@ -516,8 +520,8 @@ int kore_plan_estimate_bytes(const kore_pencil_desc *d, int precision, int nshif
     lu = std::max<int64_t>(lu, 1);
     int64_t maxrow = 1;
     for (int64_t r = 0; r < d->n; ++r) maxrow = std::max<int64_t>(maxrow, d->a_indptr[r + 1] - d->a_indptr[r]);
-    const int64_t ne = nlev > 0 ? Ks[0] - Ks[0] / 2 : 0, nt = (S + 31) / 32;
-    const int64_t ell = std::max<int64_t>(ne * nt * 32 * ((maxrow + 7) & ~7LL), 1);
+    const int64_t nt = (S + 31) / 32;
+    const int64_t ell = std::max<int64_t>((nlev > 0 ? K : 0) * nt * 32 * ((maxrow + 7) & ~7LL), 1);
     const int64_t e = (precision == KORE_PREC_FP64) ? 16 : 8, c = nshift;
     int64_t b = 0;
     // plan: A (CSR, split rows, padded level-0 rows), B, permutation, vectors
@@ -540,7 +544,7 @@ int kore_plan_estimate_bytes(const kore_pencil_desc *d, int precision, int nshif
         }
         b += c * (nm / 2 * S * Kp * 4 + nm * 8 + nj * 32 + 64);   // nm / 2 planes of S x Kp floats
     }
-    b += c * (3 * np * 16 + 2 * (np / 64 + np / 8 + 1024) * 8 + (3 * nlev + 1) * K * 4 + ell * e + 128);
+    b += c * (3 * np * 16 + 2 * (np / 64 + np / 8 + 1024) * 8 + (nlev > 0 ? 3 * nlev + 2 : 1) * K * 4 + ell * e + 128);
     b += 2 * d->n * c * 16;   // kore_solve's device copies of b and x
     // Krylov basis, its copy and the projected-problem workspace
     if (ncv > 0) b += 2 * np * (int64_t)(ncv + 1) * 16 + (int64_t)(65 * 64 * 4 + 8 * 65 + 2048 * 65 + 4096) * 16;

@@ -6,8 +6,10 @@
 //     level l, odd blocks j:   z_j = D_j^-1 f_j
 //     level l, even blocks i:  f_i <- f_i - L_i z_jl - U_i z_jr        (CSR couplings at level 0)
 // the last block is solved, x_0 = D_0^-1 f_0, and the levels are unwound in reverse,
-//     level l, odd blocks j:   x_j = z_j - G_j x_jl - H_j x_jr,
-// then x <- s x.  One cooperative persistent kernel runs all phases (about 3 log2 K of
+//     level l >= 1, odd blocks j:   x_j = z_j - G_j x_jl - H_j x_jr,
+//     level 0, odd blocks j:        g_j = c_j - L_j x_{j-1} - U_j x_{j+1},  x_j = D_j^-1 g_j
+// then x <- s x.  At level 0 the couplings are sparse, so forming g_j from them and
+// multiplying by D_j^-1 reads one dense block instead of the two of G_j, H_j.  One cooperative persistent kernel runs all phases (about 3 log2 K of
 // them) as a dataflow over tiles of 32 rows: a tile starts as soon as the blocks it
 // reads are complete (per-block completion counters), and the factor blocks stream
 // from HBM through shared memory by TMA.
@@ -52,7 +54,7 @@ struct SweepArgs {
     void *f, *z, *x;                 // nshift x np reduction vectors (factor precision)
     double2 *out;                    // nshift x np
     int accumulate;
-    int *cnt;                        // completion counters: nshift x (3 nlev + 1) x K, zeroed before the launch
+    int *cnt;                        // completion counters: nshift x stages x K, zeroed before the launch
     int *err;
     const int *skip;                 // shift s is skipped when skip[s * skip_stride] != 0
     int skip_stride;
@@ -61,6 +63,15 @@ struct SweepArgs {
 };
 
 constexpr int kMaxLevels = 24;
+
+__device__ __forceinline__ void st_release_cta(long long *p, long long v) {
+    asm volatile("st.release.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(p)), "l"(v) : "memory");
+}
+__device__ __forceinline__ long long ld_acquire_cta(const long long *p) {
+    long long v;
+    asm volatile("ld.acquire.cta.shared::cta.b64 %0, [%1];" : "=l"(v) : "r"(smem_u32(p)) : "memory");
+    return v;
+}
 
 // Thread 0 waits (bounded) until *c >= target; on timeout or an earlier error the
 // error flag is set and the caller goes on (its result is then wrong, but the kernel
@@ -77,8 +88,9 @@ __device__ __forceinline__ void wait_count(const int *c, int target, int *err) {
 
 // ----------------------------------------------------------------------------- the sweep kernel
 // The tiles (32 rows of one block) of all stages are numbered in a topological order
-//     A_0, B_0, A_1, B_1, ..., A_{L-1}, B_{L-1}, top, C_{L-1}, ..., C_0
-// (A: z_j = D_j^-1 f_j, B: f_i -= L_i z_jl + U_i z_jr, C: x_j = z_j - G_j x_jl - H_j x_jr)
+//     A_0, B_0, A_1, B_1, ..., A_{L-1}, B_{L-1}, top, C_{L-1}, ..., C_1, E_0, C_0
+// (A: z_j = D_j^-1 f_j, B: f_i -= L_i z_jl + U_i z_jr, C: x_j = z_j - G_j x_jl - H_j x_jr
+// at levels >= 1; E_0: g_j = c_j - L_j x_jl - U_j x_jr and C_0: x_j = D_j^-1 g_j)
 // and CTA c takes tiles c, c + G, c + 2G, ...  A tile waits only for the counters of
 // the blocks it reads (e.g. a B tile for A of its two neighbours), and after writing
 // its rows it adds 1 to the counter of (stage, block).  Tiles are taken in increasing
@@ -93,15 +105,16 @@ __device__ __forceinline__ void wait_count(const int *c, int target, int *err) {
 // consumer warp).  The producer runs ahead through the CTA's tile sequence: the factor
 // data of later tiles does not depend on the sweep, so it is fetched while the eight
 // consumer warps wait for their input vectors.  Several hundred KB per SM are in
-// flight without holding registers.  B_0 reads the level-0 couplings as padded rows
-// (at most a few dozen entries per row) with plain coalesced loads instead.
+// flight without holding registers.  B_0 and E_0 read the level-0 couplings as padded
+// rows (at most a few dozen entries per row) with plain coalesced loads instead.
 constexpr int kTmaConsumerWarps = 8;
 constexpr int kTmaConsumers = 32 * kTmaConsumerWarps;
-constexpr int kTmaThreads = kTmaConsumers + 32;   // + one producer warp
+constexpr int kTmaThreads = kTmaConsumers + 64;   // + one producer warp + one dependency-checker warp
 constexpr int kChunkBytes = 16384;
 constexpr int kTileRows = 32;
 constexpr int kMaxRing = 13;
 constexpr int kEllReg = 4;   // level-0 coupling entries per thread held in registers (width 32)
+constexpr int kFill = 4;     // input-vector loads in flight per consumer lane
 
 enum { kMapDinv = 0, kMapG = 1, kMapH = 2, kMapLU = 3 };
 
@@ -116,8 +129,8 @@ template <typename C> struct TmaShape {
     static constexpr int kColsPerWarp = kCols / kTmaConsumerWarps;
 };
 
-// One tile of the sweep: stage kind (0 A, 1 B, 2 top, 3 C), level, shift, block of its
-// rows, first row, and the blocks it multiplies (map, block index within the map).
+// One tile of the sweep: stage kind (0 A, 1 B, 2 top, 3 C, 4 E_0), level, shift, block
+// of its rows, first row, and the blocks it multiplies (map, block index within the map).
 struct TileJob {
     int kind, l, nmat, r0;
     int64_t s, blk;
@@ -133,8 +146,10 @@ __device__ __forceinline__ void decode_tile(int64_t g, int &k, const int64_t *st
     const int64_t loc = g - st_begin[k];
     if (k < 2 * L) { t.kind = (k & 1) ? 1 : 0; t.l = k >> 1; }
     else if (k == 2 * L) { t.kind = 2; t.l = L; }
-    else { t.kind = 3; t.l = L - 1 - (k - 2 * L - 1); }
-    const int nblk = (t.kind == 0 || t.kind == 3) ? lv_s[t.l].nodd : (t.kind == 1 ? lv_s[t.l].neven : 1);
+    else if (k < 3 * L) { t.kind = 3; t.l = 3 * L - k; }
+    else if (k == 3 * L) { t.kind = 4; t.l = 0; }
+    else { t.kind = 3; t.l = 0; }
+    const int nblk = (t.kind == 1) ? lv_s[t.l].neven : (t.kind == 2 ? 1 : lv_s[t.l].nodd);
     t.s = loc / ((int64_t)nblk * ntile);
     const int64_t rem = loc - t.s * nblk * ntile;
     const int64_t bi = rem / ntile;
@@ -164,13 +179,25 @@ __device__ __forceinline__ void decode_tile(int64_t g, int &k, const int64_t *st
     } else if (t.kind == 2) {
         t.blk = 0;
         t.map[0] = kMapDinv; t.mblk[0] = 0; t.vblk[0] = 0; t.nmat = 1;
-    } else {
+    } else if (t.kind == 3 && t.l > 0) {
         const BcrLevel lv = lv_s[t.l];
         const int64_t q = 2 * bi + 1, j = q * lv.stride;
         t.blk = j;
         t.hasr = q + 1 < lv.Kl;
         t.map[0] = kMapG; t.mblk[0] = j; t.vblk[0] = j - lv.stride; t.nmat = 1;
         if (t.hasr) { t.map[1] = kMapH; t.mblk[1] = j; t.vblk[1] = j + lv.stride; t.nmat = 2; }
+    } else if (t.kind == 3) {
+        // C_0: x_j = D_j^-1 g_j, g_j from E_0 in f
+        const int64_t j = 2 * bi + 1;
+        t.blk = j;
+        t.map[0] = kMapDinv; t.mblk[0] = j; t.vblk[0] = j; t.nmat = 1;
+    } else {
+        // E_0: g_j = c_j - L_j x_{j-1} - U_j x_{j+1} from the padded coupling rows
+        const int64_t q = 2 * bi + 1;
+        t.blk = q;
+        t.hasl = true;
+        t.hasr = q + 1 < lv_s[0].Kl;
+        t.vblk[0] = q - 1; t.vblk[1] = q + 1;
     }
 }
 
@@ -187,10 +214,11 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_sweep_tma(const __grid_const
     unsigned char *ring = smem_raw;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)nst * kChunkBytes);
     uint64_t *empty = full + nst;
-    C *vbuf = reinterpret_cast<C *>(empty + nst);   // 2 x nvec
-    __shared__ C red[kTmaConsumerWarps][33];
+    C *vbuf = reinterpret_cast<C *>(empty + nst);   // 2 x nvec input vectors (each warp fills its columns)
+    __shared__ C red[2][kTmaConsumerWarps][33];   // per-warp partial sums, by tile parity
     __shared__ BcrLevel lv_s[kMaxLevels];
     __shared__ int64_t st_begin[3 * kMaxLevels + 2];
+    __shared__ long long ready;      // highest tile of this CTA whose inputs are complete
     if (a.skip) {
         bool all = true;
         for (int s = 0; s < ns; ++s) all = all && (a.skip[s * a.skip_stride] != 0);
@@ -200,11 +228,12 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_sweep_tma(const __grid_const
     if (a.count && blockIdx.x == 0 && tid == 0) { atomicAdd(a.count, 1); atomicAdd(a.count_total, 1); }
     const int64_t np = (int64_t)K * S;
     const int ntile = (S + kTileRows - 1) / kTileRows;
-    const int nstage = 3 * L + 1;
+    const int nstage = L > 0 ? 3 * L + 2 : 1;
     if (tid < L) lv_s[tid] = a.levs[tid];
     if (tid == 0) {
         for (int i = 0; i < nst; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], kTmaConsumerWarps); }
         mbar_fence_init();
+        ready = -1;
     }
     if (tid == kTmaConsumers) for (int i = 0; i < 4; ++i) tma_prefetch_desc(&P.maps[i]);
     __syncthreads();
@@ -215,7 +244,8 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_sweep_tma(const __grid_const
             int nblk;
             if (k < 2 * L) nblk = (k & 1) ? lv_s[k >> 1].neven : lv_s[k >> 1].nodd;
             else if (k == 2 * L) nblk = 1;
-            else nblk = lv_s[L - 1 - (k - 2 * L - 1)].nodd;
+            else if (k < 3 * L) nblk = lv_s[3 * L - k].nodd;
+            else nblk = lv_s[0].nodd;   // E_0, C_0
             acc += (int64_t)nblk * ntile * ns;
         }
         st_begin[nstage] = acc;
@@ -223,6 +253,12 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_sweep_tma(const __grid_const
     __syncthreads();
     const int64_t total = st_begin[nstage];
     auto live = [&](int64_t s) -> bool { return !(a.skip && a.skip[s * a.skip_stride] != 0); };
+    auto ctr = [&](int64_t s, int sid, int64_t blk) -> int * { return a.cnt + ((s * nstage + sid) * K + blk); };
+    auto xready = [&](int64_t s, int64_t blk) -> int * {
+        if (blk == 0) return ctr(s, 2 * L, 0);
+        const int lb = __ffsll(blk) - 1;
+        return ctr(s, 2 * L + 1 + lb, blk);
+    };
 
     if (w == kTmaConsumerWarps) {
         // ------------------------------------------------------------------ producer
@@ -254,41 +290,83 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_sweep_tma(const __grid_const
         }
         return;
     }
-
-    // ---------------------------------------------------------------------- consumers
-    auto ctr = [&](int64_t s, int sid, int64_t blk) -> int * { return a.cnt + ((s * nstage + sid) * K + blk); };
     auto vec = [&](void *base, int64_t s) -> C * { return static_cast<C *>(base) + s * np; };
     auto rhs0 = [&](int64_t s, int64_t p) -> C {
         const double bn = a.bnorm[s];
         const double bscale = (bn > 0.0) ? 1.0 / bn : 1.0;
         return from_c128<C>((a.rscale[s * np + p] * bscale) * a.b[s * np + p]);
     };
-    auto emit = [&](int64_t s, int64_t p, C val) {
+
+    if (w == kTmaConsumerWarps + 1) {
+        // ------------------------------------------------------------------ dependency checker
+        // Runs ahead of the consumers through the CTA's tiles: waits (bounded, one lane
+        // per counter) for the completion counters of the blocks a tile reads and
+        // publishes the tile in `ready`, so that the consumers find their inputs complete
+        // without a round trip to global memory of their own.  A timed-out wait sets the
+        // error flag and the tile is published all the same.
+        int k = 0;
+        TileJob t;
+        for (int64_t g = blockIdx.x; g < total; g += gridDim.x) {
+            decode_tile(g, k, st_begin, lv_s, L, ntile, t);
+            const int64_t s = t.s;
+            if (live(s)) {
+                // the counters this tile needs (at most three), one lane waiting on each
+                const int *d0 = nullptr, *d1 = nullptr, *d2 = nullptr;
+                if (t.kind == 0) {
+                    if (t.l > 0) d0 = ctr(s, L + t.l - 1, t.blk);
+                } else if (t.kind == 1) {
+                    const int64_t st = lv_s[t.l].stride;
+                    if (t.hasl) d0 = ctr(s, t.l, t.blk - st);
+                    if (t.hasr) d1 = ctr(s, t.l, t.blk + st);
+                    if (t.l > 0) d2 = ctr(s, L + t.l - 1, t.blk);
+                } else if (t.kind == 2) {
+                    if (L > 0) d0 = ctr(s, 2 * L - 1, 0);
+                } else if (t.kind == 4) {
+                    d0 = xready(s, t.vblk[0]);
+                    if (t.hasr) d1 = xready(s, t.vblk[1]);
+                } else if (t.l == 0) {
+                    d0 = ctr(s, 3 * L + 1, t.blk);
+                } else {
+                    d0 = xready(s, t.vblk[0]);
+                    if (t.nmat > 1) d1 = xready(s, t.vblk[1]);
+                }
+                const int *mine = lane == 0 ? d0 : (lane == 1 ? d1 : (lane == 2 ? d2 : nullptr));
+                if (mine) wait_count(mine, ntile, a.err);
+                __syncwarp();
+            }
+            if (lane == 0) st_release_cta(&ready, (long long)g);
+        }
+        return;
+    }
+
+    // ---------------------------------------------------------------------- consumers
+    // Each warp follows the CTA's tiles on its own: it waits for `ready`, loads the
+    // entries of the input vectors that its columns of the chunks multiply, consumes
+    // its columns of every chunk of the ring, and leaves its partial sums in red; one
+    // named barrier per tile gathers them, after which warp 0 reduces and writes the
+    // rows and signals the tile's completion while the other warps go on.
+    auto emit = [&](int64_t s, int64_t p, C val, double2 prev) {
         stcg(vec(a.x, s) + p, val);
         const double bn = a.bnorm[s];
         const double2 d = ((bn > 0.0) ? bn : 1.0) * to_c128(val);
-        double2 *o = a.out + s * np + p;
-        *o = a.accumulate ? *o + d : d;
-    };
-    auto xready = [&](int64_t s, int64_t blk) -> int * {
-        if (blk == 0) return ctr(s, 2 * L, 0);
-        const int lb = __ffsll(blk) - 1;
-        return ctr(s, 2 * L + 1 + lb, blk);
+        a.out[s * np + p] = a.accumulate ? prev + d : d;
     };
     uint32_t slot = 0, ph = 0;
     int k = 0;
     TileJob t;
-    for (int64_t g = blockIdx.x; g < total; g += gridDim.x) {
+    int64_t i = 0;
+    for (int64_t g = blockIdx.x; g < total; g += gridDim.x, ++i) {
         decode_tile(g, k, st_begin, lv_s, L, ntile, t);
         const int64_t s = t.s;
-        const int sid = t.kind == 0 ? t.l : (t.kind == 1 ? L + t.l : (t.kind == 2 ? 2 * L : 2 * L + 1 + t.l));
+        const int sid = t.kind == 0 ? t.l
+                      : (t.kind == 1 ? L + t.l : (t.kind == 2 ? 2 * L : (t.kind == 3 ? 2 * L + 1 + t.l : 3 * L + 1)));
         int *done = ctr(s, sid, t.blk);
-        named_sync(1, kTmaConsumers);   // vectors of the previous tile are no longer read
+        C (*rd)[33] = red[i & 1];
         if (live(s)) {
-            // level-0 couplings (B_0): this thread's padded entries are loaded before the
-            // wait, as they do not depend on the sweep; lane = row, warp w = entries w + 8u
-            const bool ell = t.kind == 1 && t.l == 0;
-            const int64_t ebase = ((t.blk / 2) * ntile + t.r0 / kTileRows) * (int64_t)a.ell_w * 32 + lane;
+            // level-0 couplings (B_0, E_0): this thread's padded entries are loaded before
+            // the wait, as they do not depend on the sweep; lane = row, warp w = entries w + 8u
+            const bool ell = (t.kind == 1 && t.l == 0) || t.kind == 4;
+            const int64_t ebase = (t.blk * ntile + t.r0 / kTileRows) * (int64_t)a.ell_w * 32 + lane;
             const C *ellv = static_cast<const C *>(a.ell_val) + s * a.ell_stride;
             int ecol[kEllReg];
             C eval[kEllReg];
@@ -299,25 +377,61 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_sweep_tma(const __grid_const
                 ecol[u] = in ? __ldg(a.ell_col + ebase + (int64_t)kk * 32) : -1;
                 eval[u] = in ? ldg(ellv + ebase + (int64_t)kk * 32) : czero<C>();
             }
-            if (tid == 0) {
-                if (t.kind == 0) {
-                    if (t.l > 0) wait_count(ctr(s, L + t.l - 1, t.blk), ntile, a.err);
-                } else if (t.kind == 1) {
-                    const int64_t st = lv_s[t.l].stride;
-                    if (t.hasl) wait_count(ctr(s, t.l, t.blk - st), ntile, a.err);
-                    if (t.hasr) wait_count(ctr(s, t.l, t.blk + st), ntile, a.err);
-                    if (t.l > 0) wait_count(ctr(s, L + t.l - 1, t.blk), ntile, a.err);
-                } else if (t.kind == 2) {
-                    if (L > 0) wait_count(ctr(s, 2 * L - 1, 0), ntile, a.err);
-                } else {
-                    wait_count(xready(s, t.vblk[0]), ntile, a.err);
-                    if (t.nmat > 1) wait_count(xready(s, t.vblk[1]), ntile, a.err);
+            if (lane == 0) {
+                // the checker has seen this tile's inputs complete (acquire; __syncwarp
+                // orders the rest of the warp after this lane)
+                unsigned spins = 0;
+                while (ld_acquire_cta(&ready) < (long long)g) {
+                    if (++spins > KORE_SPIN_LIMIT) { atomicCAS(a.err, 0, KORE_DEVERR_FLAG); break; }
+                    __nanosleep(16);
                 }
             }
-            named_sync(1, kTmaConsumers);
+            __syncwarp();
+            // rows this tile writes, and what the write combines with (read early)
+            const int r = t.r0 + lane;
+            const int64_t p = t.blk * S + r;
+            const bool wr = w == 0 && r < S;
+            C zf = czero<C>();
+            double2 prev = mk(0.0, 0.0);
+            if (wr) {
+                if (t.kind == 1 && t.l > 0) zf = ldcg(vec(a.f, s) + p);
+                else if (t.kind == 3 && t.l > 0) zf = ldcg(vec(a.z, s) + p);
+                if ((t.kind == 2 || t.kind == 3) && a.accumulate) prev = a.out[s * np + p];
+            }
+            if (!ell && t.nmat > 0) {
+                // this warp's slice of the input vectors: columns ch kCols + w kCpw + u
+                const C *src = (t.kind == 0 || t.kind == 2 || (t.kind == 3 && t.l == 0))
+                                   ? vec(a.f, s) : (t.kind == 1 ? vec(a.z, s) : vec(a.x, s));
+                const bool from_b = (t.kind == 0 && t.l == 0) || (t.kind == 2 && L == 0);
+                const double bn = a.bnorm[s];
+                const double bscale = (bn > 0.0) ? 1.0 / bn : 1.0;
+                const int per = nc * kCpw, ne = t.nmat * per;
+                const int64_t vb0 = t.vblk[0] * S, vb1 = t.vblk[1] * S;
+                for (int e0 = 0; e0 < ne; e0 += 32 * kFill) {
+                    C v[kFill];
+                    int cv[kFill];
+#pragma unroll
+                    for (int u = 0; u < kFill; ++u) {
+                        const int e = e0 + u * 32 + lane;
+                        const int m = e >= per ? 1 : 0, rem = e - m * per;
+                        const int c = (rem / kCpw) * kCols + w * kCpw + rem % kCpw;
+                        cv[u] = (e < ne) ? m * nvec + c : -1;
+                        v[u] = czero<C>();
+                        if (e < ne && c < S) {
+                            const int64_t q = (m ? vb1 : vb0) + c;
+                            v[u] = from_b ? from_c128<C>((a.rscale[s * np + q] * bscale) * a.b[s * np + q])
+                                          : ldcg(src + q);
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < kFill; ++u)
+                        if (cv[u] >= 0) vbuf[cv[u]] = v[u];
+                }
+                __syncwarp();
+            }
+            C acc = czero<C>();
             if (ell) {
-                const C *z = vec(a.z, s);
-                C acc = czero<C>();
+                const C *z = vec(t.kind == 4 ? a.x : a.z, s);   // E_0 couples to x, B_0 to z
 #pragma unroll
                 for (int u = 0; u < kEllReg; ++u)
                     if (ecol[u] >= 0) acc = cfma(acc, eval[u], ldcg(z + ecol[u]));
@@ -325,33 +439,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_sweep_tma(const __grid_const
                     const int c = __ldg(a.ell_col + ebase + (int64_t)kk * 32);
                     if (c >= 0) acc = cfma(acc, ldg(ellv + ebase + (int64_t)kk * 32), ldcg(z + c));
                 }
-                red[w][lane] = acc;
-                named_sync(1, kTmaConsumers);
-                if (w == 0) {
-                    C val = czero<C>();
-#pragma unroll
-                    for (int q = 0; q < kTmaConsumerWarps; ++q) val = val + red[q][lane];
-                    const int r = t.r0 + lane;
-                    if (r < S) {
-                        const int64_t p = t.blk * S + r;
-                        stcg(vec(a.f, s) + p, rhs0(s, p) - val);
-                    }
-                }
             } else if (t.nmat > 0) {
-                // input vectors (zero past S: the chunk columns past S are zero too)
-                const C *src = (t.kind == 0 || t.kind == 2) ? vec(a.f, s) : (t.kind == 1 ? vec(a.z, s) : vec(a.x, s));
-                const bool from_b = (t.kind == 0 && t.l == 0) || (t.kind == 2 && L == 0);
-#pragma unroll
-                for (int m = 0; m < 2; ++m) {
-                    if (m >= t.nmat) break;
-                    for (int c = tid; c < nvec; c += kTmaConsumers) {
-                        C v = czero<C>();
-                        if (c < S) v = from_b ? rhs0(s, t.vblk[m] * S + c) : ldcg(src + t.vblk[m] * S + c);
-                        vbuf[m * nvec + c] = v;
-                    }
-                }
-                named_sync(1, kTmaConsumers);
-                C acc = czero<C>();
 #pragma unroll
                 for (int m = 0; m < 2; ++m) {
                     if (m >= t.nmat) break;
@@ -368,27 +456,28 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_sweep_tma(const __grid_const
                         if (++slot == (uint32_t)nst) { slot = 0; ph ^= 1; }
                     }
                 }
-                red[w][lane] = acc;
-                named_sync(1, kTmaConsumers);
-                if (w == 0) {
-                    C val = czero<C>();
+            }
+            rd[w][lane] = acc;
+            named_sync(1, kTmaConsumers);
+            if (w == 0) {
+                C val = czero<C>();
 #pragma unroll
-                    for (int q = 0; q < kTmaConsumerWarps; ++q) val = val + red[q][lane];
-                    const int r = t.r0 + lane;
-                    if (r < S) {
-                        const int64_t p = t.blk * S + r;
-                        if (t.kind == 0) stcg(vec(a.z, s) + p, val);
-                        else if (t.kind == 1) stcg(vec(a.f, s) + p, ldcg(vec(a.f, s) + p) - val);
-                        else if (t.kind == 2) emit(s, p, val);
-                        else emit(s, p, ldcg(vec(a.z, s) + p) - val);
-                    }
+                for (int q = 0; q < kTmaConsumerWarps; ++q) val = val + rd[q][lane];
+                if (wr) {
+                    if (ell) stcg(vec(a.f, s) + p, rhs0(s, p) - val);
+                    else if (t.kind == 0) stcg(vec(a.z, s) + p, val);
+                    else if (t.kind == 1) stcg(vec(a.f, s) + p, zf - val);
+                    else if (t.kind == 2 || t.l == 0) emit(s, p, val, prev);
+                    else emit(s, p, zf - val, prev);
                 }
             }
         }
-        named_sync(1, kTmaConsumers);
-        if (tid == 0) {
-            __threadfence();
-            atomicAdd(done, 1);
+        if (w == 0) {
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence();
+                atomicAdd(done, 1);
+            }
         }
     }
 }
@@ -621,20 +710,23 @@ int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st) {
     int smem_sm = 0, smem_blk = 0;
     KORE_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, p->device));
     KORE_CUDA_TRY(cudaDeviceGetAttribute(&smem_blk, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
-    const size_t static_smem = 8 * 1024;   // reduction tile, level table, stage offsets, per-CTA reserve
-    const size_t budget = std::min<size_t>((size_t)smem_sm / kTmaCtasPerSm, (size_t)smem_blk) - static_smem;
+    auto kern = k_sweep_tma<C>;
+    cudaFuncAttributes fa;
+    KORE_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
+    const size_t static_smem = fa.sharedSizeBytes + 1024;   // + the per-CTA reserve of the SM
+    const size_t budget = std::min<size_t>((size_t)smem_sm / kTmaCtasPerSm - static_smem,
+                                           (size_t)smem_blk - fa.sharedSizeBytes);
     int nst = kMaxRing;
     while (nst > 2 && tma_smem<C>(p->S, nst) > budget) --nst;
     if (tma_smem<C>(p->S, nst) > budget) return KORE_EINVAL;
     P.nst = nst;
     const size_t smem = tma_smem<C>(p->S, nst);
-    auto kern = k_sweep_tma<C>;
     KORE_TRY(kore_allow_max_dyn_smem(kern, p->device));
     int occ = 0;
     KORE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTmaThreads, smem));
     if (occ < 1) return KORE_EINVAL;
     occ = std::min(occ, kTmaCtasPerSm);
-    KORE_CUDA_TRY(cudaMemsetAsync(a.cnt, 0, (size_t)ns * (3 * p->nlev + 1) * p->K * sizeof(int), st));
+    KORE_CUDA_TRY(cudaMemsetAsync(a.cnt, 0, (size_t)ns * p->sweep_stages() * p->K * sizeof(int), st));
     void *args[] = {&P};
     dim3 grid(p->num_sms * occ), block(kTmaThreads);
     KORE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)kern, grid, block, args, smem, st));
@@ -871,7 +963,7 @@ int kore_ir_read(kore_plan *p, IrState *out) {
 namespace {
 
 constexpr int64_t kNoAllocMaxNp = 16384;
-constexpr int64_t kNoAllocMaxCnt = 32768;   // sweep completion counters: (3 levels + 1) x blocks
+constexpr int64_t kNoAllocMaxCnt = 32768;   // sweep completion counters: (3 levels + 2) x blocks
 constexpr int64_t kNoAllocMaxSpmvCta = (kNoAllocMaxNp * kRowLanes + 255) / 256 + kNoAllocMaxNp / 8 + 1;
 
 struct NoAllocScratch {
@@ -963,7 +1055,7 @@ int noalloc_solve(kore_plan *p, NoAllocScratch *s, const double2 *b_dev, double2
 
 extern "C" int kore_solve_dev_noalloc(kore_plan *p, const void *b_dev, void *x_dev, double refine_tol, void *stream) {
     if (!p || !b_dev || !x_dev) return KORE_EINVAL;
-    if (p->np > kNoAllocMaxNp || (int64_t)(3 * p->nlev + 1) * p->K > kNoAllocMaxCnt) {
+    if (p->np > kNoAllocMaxNp || (int64_t)p->sweep_stages() * p->K > kNoAllocMaxCnt) {
         std::fprintf(stderr,
                      "kore_solve_dev_noalloc: %lld padded unknowns in %d blocks exceed the fixed scratch "
                      "(%lld unknowns, %lld block counters); use kore_solve_dev\n",
