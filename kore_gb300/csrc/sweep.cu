@@ -587,6 +587,40 @@ __device__ __forceinline__ void row_dot(const SpmvArgs &a, int64_t p, int sub, c
     if (a.has_b) seg_dot<LANES>(a.bcol, a.bval, a.brow[p], a.brow[p + 1], sub, x, sb);
 }
 
+// |v| of a double as the bits of its absolute value: for non-negative IEEE doubles the
+// integer order is the numeric order, so maxima run on the integer units, not on the
+// FP64 pipe, and a NaN (above +inf as bits) is kept instead of dropped as fmax drops it
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Sum of the partial sums a[0..5] of the kRowLanes (= 4) lanes of a row, with 6 FP64
+// additions per lane instead of 12: the lanes first exchange halves of their values
+// (each adds three), then the pairs add their three; lane sub = 0 of the row ends with
+// a[0..2], lane 1 with a[3..5], and lane 0 fetches those.
+__device__ __forceinline__ void row_reduce4(double (&a)[6], int sub) {
+    const bool odd = sub & 1;
+    double k[3];
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+        const double send = odd ? a[u] : a[u + 3];
+        const double keep = odd ? a[u + 3] : a[u];
+        k[u] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+    }
+#pragma unroll
+    for (int u = 0; u < 3; ++u) k[u] += __shfl_xor_sync(0xffffffffu, k[u], 2);
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+        const double hi = __shfl_down_sync(0xffffffffu, k[u], 1);   // lane sub + 1's sums
+        a[u] = k[u];
+        a[u + 3] = hi;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
     const int64_t s = blockIdx.y;
     if (a.skip && a.skip[s * a.skip_stride]) return;
@@ -595,14 +629,15 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
     double2 *y = a.y + s * np;
     const double2 *rhs = a.rhs ? a.rhs + s * np : nullptr;
     const double2 lam = a.sig ? a.sig[s] : a.lam;
-    double rmax = 0.0, xmax = 0.0;
+    unsigned long long rmax = 0, xmax = 0;
     auto finish = [&](int64_t p, double2 sr, double2 si, double2 sb) {
         const double2 sa = mk(sr.x - si.y, sr.y + si.x);   // A x = sr + i si
         double2 v = (a.mode == 0) ? sb : sa - lam * sb;
         if (a.mode == 2) {
             v = rhs[p] - v;
-            rmax = fmax(rmax, fmax(fabs(v.x), fabs(v.y)));
-            xmax = fmax(xmax, fmax(fabs(x[p].x), fabs(x[p].y)));
+            const double2 xp = x[p];
+            rmax = max(rmax, max(abs_bits(v.x), abs_bits(v.y)));
+            xmax = max(xmax, max(abs_bits(xp.x), abs_bits(xp.y)));
         }
         y[p] = v;
     };
@@ -616,12 +651,11 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
         }
         double2 sr = mk(0.0, 0.0), si = mk(0.0, 0.0), sb = mk(0.0, 0.0);
         if (live) row_dot<kRowLanes>(a, p, sub, x, sr, si, sb);
-#pragma unroll
-        for (int o = kRowLanes / 2; o > 0; o >>= 1) {
-            sr = sr + shfl_down_w(sr, o, kRowLanes);
-            si = si + shfl_down_w(si, o, kRowLanes);
-            sb = sb + shfl_down_w(sb, o, kRowLanes);
-        }
+        double part[6] = {sr.x, sr.y, si.x, si.y, sb.x, sb.y};
+        row_reduce4(part, sub);
+        sr = mk(part[0], part[1]);
+        si = mk(part[2], part[3]);
+        sb = mk(part[4], part[5]);
         if (live && sub == 0) finish(p, sr, si, sb);
     } else {
         const int lane = threadIdx.x & 31;
@@ -637,15 +671,15 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
         }
     }
     if (a.mode == 2) {
-        rmax = warp_max_d(rmax);
-        xmax = warp_max_d(xmax);
-        __shared__ double sm[2][8];
+        rmax = warp_max_bits(rmax);
+        xmax = warp_max_bits(xmax);
+        __shared__ unsigned long long sm[2][8];
         if ((threadIdx.x & 31) == 0) { sm[0][threadIdx.x >> 5] = rmax; sm[1][threadIdx.x >> 5] = xmax; }
         __syncthreads();
         if (threadIdx.x == 0) {
-            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { rmax = fmax(rmax, sm[0][w]); xmax = fmax(xmax, sm[1][w]); }
-            a.part[s * 2 * gridDim.x + 2 * blockIdx.x] = rmax;
-            a.part[s * 2 * gridDim.x + 2 * blockIdx.x + 1] = xmax;
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { rmax = max(rmax, sm[0][w]); xmax = max(xmax, sm[1][w]); }
+            a.part[s * 2 * gridDim.x + 2 * blockIdx.x] = __longlong_as_double((long long)rmax);
+            a.part[s * 2 * gridDim.x + 2 * blockIdx.x + 1] = __longlong_as_double((long long)xmax);
         }
     }
 }
@@ -849,18 +883,20 @@ __global__ void k_ir_check(const double *__restrict__ part, int n, const double 
     IrState *st = stall + s;
     if (st->done) return;
     part += (int64_t)s * 2 * n;
-    double rm = 0.0, xm = 0.0;
+    // maxima of non-negative doubles as bits (a NaN among them stays, and is caught below)
+    unsigned long long rb = 0, xb = 0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        rm = fmax(rm, part[2 * i]);
-        xm = fmax(xm, part[2 * i + 1]);
+        rb = max(rb, abs_bits(part[2 * i]));
+        xb = max(xb, abs_bits(part[2 * i + 1]));
     }
-    rm = warp_max_d(rm);
-    xm = warp_max_d(xm);
-    __shared__ double s0[32], s1[32];
-    if ((threadIdx.x & 31) == 0) { s0[threadIdx.x >> 5] = rm; s1[threadIdx.x >> 5] = xm; }
+    rb = warp_max_bits(rb);
+    xb = warp_max_bits(xb);
+    __shared__ unsigned long long s0[32], s1[32];
+    if ((threadIdx.x & 31) == 0) { s0[threadIdx.x >> 5] = rb; s1[threadIdx.x >> 5] = xb; }
     __syncthreads();
     if (threadIdx.x != 0) return;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { rm = fmax(rm, s0[w]); xm = fmax(xm, s1[w]); }
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { rb = max(rb, s0[w]); xb = max(xb, s1[w]); }
+    const double rm = __longlong_as_double((long long)rb), xm = __longlong_as_double((long long)xb);
     const double den = minf[s] * xm + bnorm[s];
     const double eta = (den > 0.0) ? rm / den : 0.0;
     if (!(eta == eta)) {
