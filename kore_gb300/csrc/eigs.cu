@@ -343,11 +343,29 @@ __global__ void __launch_bounds__(kSchurT) k_schur(const double2 *__restrict__ H
 // the kernel returns at once unless *run != 0.
 constexpr int kDotThreads = 256;
 constexpr int kDotChunk = 8;
+
+// Sums of 16 values over the 32 lanes of a warp with 16 FP64 additions per lane (a
+// butterfly of 5 steps where each lane keeps half of its values and adds the partner's
+// copy of that half) instead of the 80 of 16 separate warp sums; lanes 2k and 2k + 1
+// return the total of value k.
+__device__ __forceinline__ double warp_transpose_sum16(double (&v)[16], int lane) {
+#pragma unroll
+    for (int h = 8, m = 16; h >= 1; h >>= 1, m >>= 1) {
+        const bool up = lane & m;
+#pragma unroll
+        for (int i = 0; i < h; ++i) {
+            const double send = up ? v[i] : v[i + h];
+            const double keep = up ? v[i + h] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, m);
+        }
+    }
+    return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
 __global__ void __launch_bounds__(kDotThreads) k_mdot(int64_t np, int ncol, const double2 *__restrict__ V,
                                                       const double2 *__restrict__ w, double2 *__restrict__ partial,
                                                       int with_norm, const int *__restrict__ run) {
     if (run && *run == 0) return;
-    __shared__ double2 sm[kDotThreads / 32][kDotChunk];
+    __shared__ double sm[kDotThreads / 32][2 * kDotChunk];
     const int nc = ncol + with_norm;
     for (int c0 = 0; c0 < nc; c0 += kDotChunk) {
         double2 acc[kDotChunk];
@@ -359,15 +377,18 @@ __global__ void __launch_bounds__(kDotThreads) k_mdot(int64_t np, int ncol, cons
             for (int t = 0; t < kDotChunk; ++t)
                 if (c0 + t < nc) acc[t] = cfmaconj(acc[t], (c0 + t < ncol) ? V[r + (int64_t)(c0 + t) * np] : wr, wr);
         }
+        // warp sums of the 2 kDotChunk doubles: even lane L ends with value L / 2
+        double v[2 * kDotChunk];
 #pragma unroll
-        for (int t = 0; t < kDotChunk; ++t) {
-            double2 v = warp_sum(acc[t]);
-            if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5][t] = v;
-        }
+        for (int t = 0; t < kDotChunk; ++t) { v[2 * t] = acc[t].x; v[2 * t + 1] = acc[t].y; }
+        const int lane = threadIdx.x & 31;
+        const double tot = warp_transpose_sum16(v, lane);
+        if ((lane & 1) == 0) sm[threadIdx.x >> 5][lane >> 1] = tot;
         __syncthreads();
         if (threadIdx.x < kDotChunk && c0 + (int)threadIdx.x < nc) {
             double2 s = mk(0.0, 0.0);
-            for (int wv = 0; wv < kDotThreads / 32; ++wv) s = s + sm[wv][threadIdx.x];
+            for (int wv = 0; wv < kDotThreads / 32; ++wv)
+                s = s + mk(sm[wv][2 * threadIdx.x], sm[wv][2 * threadIdx.x + 1]);
             partial[blockIdx.x * (int64_t)nc + c0 + threadIdx.x] = s;
         }
         __syncthreads();
