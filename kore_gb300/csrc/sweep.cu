@@ -107,8 +107,12 @@ __device__ __forceinline__ void wait_count(const int *c, int target, int *err) {
 // consumer warps wait for their input vectors.  Several hundred KB per SM are in
 // flight without holding registers.  B_0 and E_0 read the level-0 couplings as padded
 // rows (at most a few dozen entries per row) with plain coalesced loads instead.
-constexpr int kTmaConsumerWarps = 8;
+constexpr int kTmaConsumerWarps = 4;
 constexpr int kTmaConsumers = 32 * kTmaConsumerWarps;
+// CTAs per SM: three CTAs of three or four 16 KB slots keep ~200 KB per SM in flight,
+// and a CTA's per-tile work (input vectors, reduction, signalling) overlaps the other
+// CTAs' streaming
+constexpr int kTmaCtasPerSm = 3;
 constexpr int kTmaThreads = kTmaConsumers + 64;   // + one producer warp + one dependency-checker warp
 constexpr int kChunkBytes = 16384;
 constexpr int kTileRows = 32;
@@ -202,7 +206,7 @@ __device__ __forceinline__ void decode_tile(int64_t g, int &k, const int64_t *st
 }
 
 template <typename C>
-__global__ void __launch_bounds__(kTmaThreads, 2) k_sweep_tma(const __grid_constant__ SweepTmaParams P) {
+__global__ void __launch_bounds__(kTmaThreads, kTmaCtasPerSm) k_sweep_tma(const __grid_constant__ SweepTmaParams P) {
     using Shape = TmaShape<C>;
     constexpr int kCols = Shape::kCols, kCpw = Shape::kColsPerWarp;
     const SweepArgs &a = P.a;
@@ -702,10 +706,6 @@ __global__ void k_scatter(int64_t np, int64_t n, const int64_t *__restrict__ s2o
     }
 }
 
-// Ring slots and CTAs per SM of the tensor-copy sweep: two CTAs of six 16 KB slots
-// each keep ~200 KB per SM in flight and let one CTA compute while the other waits
-// for its inputs.
-constexpr int kTmaCtasPerSm = 2;
 
 template <typename C>
 size_t tma_smem(int S, int nst) {
