@@ -50,10 +50,10 @@ FORCED = {
 
 
 # DRAM traffic of one sweep launch over its algorithmic bytes, from one ncu capture of
-# the 120-block shell (dram__bytes_read.sum + dram__bytes_write.sum = 612.5 MB against
-# 627.1 MB; profiles/k_sweep_tma_shell_lmax121_mixed.md).  Both grow with the block
+# the 120-block shell (dram__bytes_read.sum + dram__bytes_write.sum = 542.4 MB against
+# 551.7 MB; profiles/k_sweep_tma_shell_lmax121_mixed.md).  Both grow with the block
 # count, so the ratio carries over to the 600-block workload.
-SWEEP_TRAFFIC_RATIO = 612.5 / 627.1
+SWEEP_TRAFFIC_RATIO = 542.4 / 551.7
 
 
 def describe(w):
@@ -590,7 +590,7 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "k_sweep_tma (block-tridiagonal forward+back sweep, TMA-fed dataflow)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": src, "traffic": SWEEP_TRAFFIC_RATIO * prof["sweep_bytes"],
-                     "traffic_source": "dram bytes read + written / algorithmic bytes = 612.5 MB / 627.1 MB in one "
+                     "traffic_source": "dram bytes read + written / algorithmic bytes = 542.4 MB / 551.7 MB in one "
                                        "ncu capture of the 120-block case, scaled by the block count",
                      "bytes_per_launch": prof["sweep_bytes"],
                      "avg_launch_ms": sweep_ms, "launches": prof["sweeps"],
