@@ -526,12 +526,13 @@ __global__ void k_reduce_max(const double *__restrict__ in, int n, double *__res
 // SM per clock), so A is stored as a real matrix split into real and imaginary
 // coefficients (two multiply-adds per value instead of four for a complex entry),
 // each row's real and imaginary segments summed separately and combined at the end.
-// Rows are short (a few dozen values): 4 lanes per row, each lane with kRowUnroll
-// gathers in flight.  The tau-method boundary rows are dense over a radial expansion
+// Rows are short (a few dozen values): 2 lanes per row, each lane with kRowUnroll
+// gathers in flight (2 lanes rather than 4 halve the FP64 additions that combine a
+// row's partial sums, which cost FP64-pipe issue slots like the products do).  The tau-method boundary rows are dense over a radial expansion
 // (hundreds of entries); rows with more than kKoreLongRow values (A + B) are listed at plan
 // creation and done by a whole warp each in extra CTAs at the end of the grid, so that
 // they do not hold back the CTAs of the short rows.
-constexpr int kRowLanes = 4;
+constexpr int kRowLanes = 2;
 constexpr int kRowUnroll = 4;
 
 struct SpmvArgs {
@@ -602,11 +603,13 @@ __device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long v
     return v;
 }
 
-// Sum of the partial sums a[0..5] of the kRowLanes (= 4) lanes of a row, with 6 FP64
-// additions per lane instead of 12: the lanes first exchange halves of their values
-// (each adds three), then the pairs add their three; lane sub = 0 of the row ends with
-// a[0..2], lane 1 with a[3..5], and lane 0 fetches those.
-__device__ __forceinline__ void row_reduce4(double (&a)[6], int sub) {
+// Sum of the partial sums a[0..5] of the LANES (2 or 4) lanes of a row with 3 (or 6)
+// FP64 additions per lane instead of 6 (or 12): the lanes first exchange halves of their
+// values (each adds three), then (4 lanes) the pairs add their three; lane sub = 0 of
+// the row ends with a[0..2], lane 1 with a[3..5], and lane 0 fetches those.
+template <int LANES>
+__device__ __forceinline__ void row_reduce(double (&a)[6], int sub) {
+    static_assert(LANES == 2 || LANES == 4, "2 or 4 lanes per row");
     const bool odd = sub & 1;
     double k[3];
 #pragma unroll
@@ -615,8 +618,10 @@ __device__ __forceinline__ void row_reduce4(double (&a)[6], int sub) {
         const double keep = odd ? a[u + 3] : a[u];
         k[u] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
     }
+    if (LANES == 4) {
 #pragma unroll
-    for (int u = 0; u < 3; ++u) k[u] += __shfl_xor_sync(0xffffffffu, k[u], 2);
+        for (int u = 0; u < 3; ++u) k[u] += __shfl_xor_sync(0xffffffffu, k[u], 2);
+    }
 #pragma unroll
     for (int u = 0; u < 3; ++u) {
         const double hi = __shfl_down_sync(0xffffffffu, k[u], 1);   // lane sub + 1's sums
@@ -656,7 +661,7 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
         double2 sr = mk(0.0, 0.0), si = mk(0.0, 0.0), sb = mk(0.0, 0.0);
         if (live) row_dot<kRowLanes>(a, p, sub, x, sr, si, sb);
         double part[6] = {sr.x, sr.y, si.x, si.y, sb.x, sb.y};
-        row_reduce4(part, sub);
+        row_reduce<kRowLanes>(part, sub);
         sr = mk(part[0], part[1]);
         si = mk(part[2], part[3]);
         sb = mk(part[4], part[5]);

@@ -61,6 +61,26 @@ def test_forced_problem(gpu_lib, case, precision):
     assert np.isfinite(x).all()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_forced_nan_rhs_reports_enan(gpu_lib, case, precision):
+    """A NaN in the right-hand side ends the solve with KORE_ENAN, as bin/solve.py:263-268
+    stops on a NaN solution.  In mixed precision the refinement's residual maxima are
+    taken on the bits of |r|, which keep a NaN (fmax would drop it), so the loop stops
+    at its first check."""
+    from kore_gb300 import KSP
+    from kore_gb300._lib import KoreError
+    meta, A, bf = case("forced_m2_f10")
+    b = bf.toarray().ravel().astype(complex)
+    b[len(b) // 2] = np.nan
+    with make_pencil(meta, A, bf) as p:
+        k = KSP()
+        k.setOperators(p)
+        k.setFromOptions({"kore_precision": precision})
+        with pytest.raises(KoreError) as e:
+            k.solve(b)
+    assert e.value.status == 8   # KORE_ENAN
+
+
 def run_eps(p, meta, precision, which=None, nev=None, seed=1):
     from kore_gb300 import EPS
     E = EPS()
