@@ -30,11 +30,6 @@ namespace {
 __device__ __forceinline__ double2 ldcg(const double2 *p) { return __ldcg(p); }
 __device__ __forceinline__ float2 ldcg(const float2 *p) { return __ldcg(p); }
 __device__ __forceinline__ double2 ldg(const double2 *p) { return __ldg(p); }
-__device__ __forceinline__ double2 shfl_down_w(double2 v, int o, int width) {
-    v.x = __shfl_down_sync(0xffffffffu, v.x, o, width);
-    v.y = __shfl_down_sync(0xffffffffu, v.y, o, width);
-    return v;
-}
 __device__ __forceinline__ float2 ldg(const float2 *p) { return __ldg(p); }
 __device__ __forceinline__ void stcg(double2 *p, double2 v) { __stcg(p, v); }
 __device__ __forceinline__ void stcg(float2 *p, float2 v) { __stcg(p, v); }
@@ -526,13 +521,14 @@ __global__ void k_reduce_max(const double *__restrict__ in, int n, double *__res
 // SM per clock), so A is stored as a real matrix split into real and imaginary
 // coefficients (two multiply-adds per value instead of four for a complex entry),
 // each row's real and imaginary segments summed separately and combined at the end.
-// Rows are short (a few dozen values): 2 lanes per row, each lane with kRowUnroll
-// gathers in flight (2 lanes rather than 4 halve the FP64 additions that combine a
-// row's partial sums, which cost FP64-pipe issue slots like the products do).  The tau-method boundary rows are dense over a radial expansion
+// Rows are short (a few dozen values): one thread per row with kRowUnroll gathers in
+// flight.  Splitting a row over 2 or 4 lanes costs FP64 additions to combine the
+// partial sums, which take FP64-pipe issue slots like the products do (measured on
+// the 240k-unknown shell: 4 lanes 179 ms, 2 lanes 140 ms, 1 lane 129 ms per solve).  The tau-method boundary rows are dense over a radial expansion
 // (hundreds of entries); rows with more than kKoreLongRow values (A + B) are listed at plan
 // creation and done by a whole warp each in extra CTAs at the end of the grid, so that
 // they do not hold back the CTAs of the short rows.
-constexpr int kRowLanes = 2;
+constexpr int kRowLanes = 1;   // threads per short row
 constexpr int kRowUnroll = 4;
 
 struct SpmvArgs {
@@ -603,33 +599,6 @@ __device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long v
     return v;
 }
 
-// Sum of the partial sums a[0..5] of the LANES (2 or 4) lanes of a row with 3 (or 6)
-// FP64 additions per lane instead of 6 (or 12): the lanes first exchange halves of their
-// values (each adds three), then (4 lanes) the pairs add their three; lane sub = 0 of
-// the row ends with a[0..2], lane 1 with a[3..5], and lane 0 fetches those.
-template <int LANES>
-__device__ __forceinline__ void row_reduce(double (&a)[6], int sub) {
-    static_assert(LANES == 2 || LANES == 4, "2 or 4 lanes per row");
-    const bool odd = sub & 1;
-    double k[3];
-#pragma unroll
-    for (int u = 0; u < 3; ++u) {
-        const double send = odd ? a[u] : a[u + 3];
-        const double keep = odd ? a[u + 3] : a[u];
-        k[u] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
-    }
-    if (LANES == 4) {
-#pragma unroll
-        for (int u = 0; u < 3; ++u) k[u] += __shfl_xor_sync(0xffffffffu, k[u], 2);
-    }
-#pragma unroll
-    for (int u = 0; u < 3; ++u) {
-        const double hi = __shfl_down_sync(0xffffffffu, k[u], 1);   // lane sub + 1's sums
-        a[u] = k[u];
-        a[u + 3] = hi;
-    }
-}
-
 __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
     const int64_t s = blockIdx.y;
     if (a.skip && a.skip[s * a.skip_stride]) return;
@@ -651,21 +620,18 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
         y[p] = v;
     };
     if ((int)blockIdx.x < a.short_blocks) {
-        const int sub = threadIdx.x & (kRowLanes - 1);
-        const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kRowLanes;
+        static_assert(kRowLanes == 1, "one thread per short row");
+        const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
         bool live = p < np;
         if (live) {
             const int len = (a.srow[p + 1] - a.srow[p]) + (a.has_b ? a.brow[p + 1] - a.brow[p] : 0);
             live = len <= kKoreLongRow;
         }
-        double2 sr = mk(0.0, 0.0), si = mk(0.0, 0.0), sb = mk(0.0, 0.0);
-        if (live) row_dot<kRowLanes>(a, p, sub, x, sr, si, sb);
-        double part[6] = {sr.x, sr.y, si.x, si.y, sb.x, sb.y};
-        row_reduce<kRowLanes>(part, sub);
-        sr = mk(part[0], part[1]);
-        si = mk(part[2], part[3]);
-        sb = mk(part[4], part[5]);
-        if (live && sub == 0) finish(p, sr, si, sb);
+        if (live) {
+            double2 sr = mk(0.0, 0.0), si = mk(0.0, 0.0), sb = mk(0.0, 0.0);
+            row_dot<1>(a, p, 0, x, sr, si, sb);
+            finish(p, sr, si, sb);
+        }
     } else {
         const int lane = threadIdx.x & 31;
         const int wid = (blockIdx.x - a.short_blocks) * (blockDim.x >> 5) + (threadIdx.x >> 5);
