@@ -157,57 +157,80 @@ int permute_csr(const kore_plan *p, const std::vector<int64_t> &orig2slot, const
     return bad ? KORE_EINVAL : KORE_OK;
 }
 
-// Padded coupling rows of the level-0 even blocks (kore_plan::d_ell_*) from the
+// Padded coupling rows of the level-0 blocks (kore_plan::d_ell_*) from the
 // permuted CSR of A: the entries left of the diagonal block, then those right of it.
 int build_ell(kore_plan *p, const std::vector<int> &row, const std::vector<int> &col, const std::vector<int> &split) {
     const int64_t S = p->S;
     const int nt = (int)((S + 31) / 32);
     const int64_t nb = p->nlev > 0 ? p->K : 0;
     int w = 1;
-    for (int64_t bi = 0; bi < nb; ++bi)
-        for (int64_t r = 0; r < S; ++r) {
-            const int64_t q = bi * S + r;
-            w = std::max(w, (split[2 * q] - row[q]) + (row[q + 1] - split[2 * q + 1]));
-        }
+#pragma omp parallel for reduction(max : w)
+    for (int64_t q = 0; q < nb * S; ++q) w = std::max(w, (split[2 * q] - row[q]) + (row[q + 1] - split[2 * q + 1]));
     p->ell_w = (w + 7) & ~7;
     p->ell_rows = nb * nt * 32;
     std::vector<int> ecol(std::max<int64_t>(p->ell_stride(), 1), -1), esrc(ecol.size(), -1);
-    for (int64_t bi = 0; bi < nb; ++bi)
-        for (int64_t r = 0; r < S; ++r) {
-            const int64_t q = bi * S + r;
-            const int64_t base = ((bi * nt + r / 32) * p->ell_w) * 32 + r % 32;
-            int k = 0;
-            auto put = [&](int e) {
-                ecol[base + (int64_t)k * 32] = col[e];
-                esrc[base + (int64_t)k * 32] = e;
-                ++k;
-            };
-            for (int e = row[q]; e < split[2 * q]; ++e) put(e);
-            for (int e = split[2 * q + 1]; e < row[q + 1]; ++e) put(e);
-            p->ell_nnz += k;
-        }
+    int64_t ennz = 0;
+#pragma omp parallel for reduction(+ : ennz)
+    for (int64_t q = 0; q < nb * S; ++q) {
+        const int64_t bi = q / S, r = q - bi * S;
+        const int64_t base = ((bi * nt + r / 32) * p->ell_w) * 32 + r % 32;
+        int k = 0;
+        auto put = [&](int e) {
+            ecol[base + (int64_t)k * 32] = col[e];
+            esrc[base + (int64_t)k * 32] = e;
+            ++k;
+        };
+        for (int e = row[q]; e < split[2 * q]; ++e) put(e);
+        for (int e = split[2 * q + 1]; e < row[q + 1]; ++e) put(e);
+        ennz += k;
+    }
+    p->ell_nnz = ennz;
     KORE_TRY(upload(p, &p->d_ell_col, ecol));
     KORE_TRY(upload(p, &p->d_ell_src, esrc));
-    // the odd blocks' couplings by column (G_j = D_j^-1 L_j, H_j = D_j^-1 U_j at level 0)
-    const int64_t no = p->nlev > 0 ? p->lev[0].nodd : 0;
-    std::vector<int> cptr(std::max<int64_t>(2 * no * (S + 1), 1), 0), crow, csrc;
-    for (int64_t o = 0; o < no; ++o)
-        for (int side = 0; side < 2; ++side) {
-            const int64_t j = 2 * o + 1, nbr = side ? j + 1 : j - 1;
-            std::vector<std::vector<std::pair<int, int>>> bycol(S);
-            for (int64_t r = 0; r < S; ++r) {
-                const int64_t q = j * S + r;
-                const int e0 = side ? split[2 * q + 1] : row[q], e1 = side ? row[q + 1] : split[2 * q];
-                for (int e = e0; e < e1; ++e) bycol[col[e] - nbr * S].push_back({(int)r, e});
-            }
-            int *ptr = &cptr[(2 * o + side) * (S + 1)];
-            ptr[0] = (int)crow.size();
-            for (int64_t c = 0; c < S; ++c) {
-                for (const auto &re : bycol[c]) { crow.push_back(re.first); csrc.push_back(re.second); }
-                ptr[c + 1] = (int)crow.size();
+    // The odd blocks' couplings by column (G_j = D_j^-1 L_j, H_j = D_j^-1 U_j at level 0):
+    // task t = 2 o + side holds the entries of block j = 2 o + 1 in the columns of its
+    // left (side 0) or right (side 1) neighbour, column by column, rows ascending.
+    // Counted per column first, then filled, each task on its own thread.
+    const int64_t no = p->nlev > 0 ? p->lev[0].nodd : 0, ntask = 2 * no;
+    std::vector<int> cptr(std::max<int64_t>(ntask * (S + 1), 1), 0);
+    auto entries = [&](int64_t t, int64_t r, int &e0, int &e1) {
+        const int64_t j = 2 * (t / 2) + 1, q = j * S + r;
+        e0 = (t & 1) ? split[2 * q + 1] : row[q];
+        e1 = (t & 1) ? row[q + 1] : split[2 * q];
+    };
+    auto nbr_of = [&](int64_t t) -> int64_t { return (t & 1) ? 2 * (t / 2) + 2 : 2 * (t / 2); };
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t t = 0; t < ntask; ++t) {
+        int *cnt = &cptr[t * (S + 1)];
+        for (int64_t r = 0; r < S; ++r) {
+            int e0, e1;
+            entries(t, r, e0, e1);
+            for (int e = e0; e < e1; ++e) ++cnt[col[e] - nbr_of(t) * S + 1];
+        }
+    }
+    // offsets: each task's columns follow the previous task's
+    int64_t total = 0;
+    for (int64_t t = 0; t < ntask; ++t) {
+        int *ptr = &cptr[t * (S + 1)];
+        ptr[0] = (int)total;
+        for (int64_t c = 0; c < S; ++c) ptr[c + 1] += ptr[c];
+        total = ptr[S];
+    }
+    std::vector<int> crow(std::max<int64_t>(total, 1), 0), csrc(crow.size(), 0);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t t = 0; t < ntask; ++t) {
+        const int *ptr = &cptr[t * (S + 1)];
+        std::vector<int> cur(ptr, ptr + S);
+        for (int64_t r = 0; r < S; ++r) {
+            int e0, e1;
+            entries(t, r, e0, e1);
+            for (int e = e0; e < e1; ++e) {
+                const int k = cur[col[e] - nbr_of(t) * S]++;
+                crow[k] = (int)r;
+                csrc[k] = e;
             }
         }
-    if (crow.empty()) { crow.push_back(0); csrc.push_back(0); }
+    }
     KORE_TRY(upload(p, &p->d_cc_ptr, cptr));
     KORE_TRY(upload(p, &p->d_cc_row, crow));
     KORE_TRY(upload(p, &p->d_cc_src, csrc));
@@ -264,21 +287,38 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
         KORE_TRY(upload(p, &p->d_aval, val));
         KORE_TRY(upload(p, &p->d_asplit, split));
         KORE_TRY(build_ell(p, row, col, split));
-        // real/imaginary split of A for the sparse products
-        std::vector<int> srow(p->np + 1, 0), smid(p->np), scol;
-        std::vector<double> sval;
-        scol.reserve(col.size() + col.size() / 2);
-        sval.reserve(col.size() + col.size() / 2);
+        // real/imaginary split of A for the sparse products: per row the values with a
+        // nonzero real part, then those with a nonzero imaginary part (counted, then
+        // filled, rows in parallel)
+        std::vector<int> srow(p->np + 1, 0), smid(p->np), nre(p->np), nim(p->np);
+#pragma omp parallel for schedule(static, 1024)
         for (int64_t q = 0; q < p->np; ++q) {
-            for (int e = row[q]; e < row[q + 1]; ++e)
-                if (val[e].x != 0.0) { scol.push_back(col[e]); sval.push_back(val[e].x); }
-            smid[q] = (int)scol.size();
-            for (int e = row[q]; e < row[q + 1]; ++e)
-                if (val[e].y != 0.0) { scol.push_back(col[e]); sval.push_back(val[e].y); }
-            srow[q + 1] = (int)scol.size();
+            int a = 0, b = 0;
+            for (int e = row[q]; e < row[q + 1]; ++e) {
+                a += val[e].x != 0.0;
+                b += val[e].y != 0.0;
+            }
+            nre[q] = a;
+            nim[q] = b;
         }
-        if (scol.size() >= (size_t)INT32_MAX) return KORE_EINVAL;
-        p->s_nnz = (int64_t)scol.size();
+        int64_t stot = 0;
+        for (int64_t q = 0; q < p->np; ++q) {
+            if (stot + nre[q] + nim[q] >= (int64_t)INT32_MAX) return KORE_EINVAL;
+            smid[q] = (int)(stot + nre[q]);
+            stot += nre[q] + nim[q];
+            srow[q + 1] = (int)stot;
+        }
+        std::vector<int> scol(std::max<int64_t>(stot, 1));
+        std::vector<double> sval(scol.size());
+#pragma omp parallel for schedule(static, 1024)
+        for (int64_t q = 0; q < p->np; ++q) {
+            int kr = srow[q], ki = smid[q];
+            for (int e = row[q]; e < row[q + 1]; ++e) {
+                if (val[e].x != 0.0) { scol[kr] = col[e]; sval[kr] = val[e].x; ++kr; }
+                if (val[e].y != 0.0) { scol[ki] = col[e]; sval[ki] = val[e].y; ++ki; }
+            }
+        }
+        p->s_nnz = stot;
         KORE_TRY(upload(p, &p->d_srow, srow));
         KORE_TRY(upload(p, &p->d_smid, smid));
         KORE_TRY(upload(p, &p->d_scol, scol));
