@@ -492,8 +492,11 @@ def main():
     fsteps = args.fp64_steps if args.fp64_steps is not None else args.steps
     lat64, pairs64, stats64 = [], 0, {}
     if fsteps > 0:
-        E64, lat64, pairs64, wall64 = time_arm(p, torch, stream, args.workload, "fp64", fsteps,
-                                               min(args.warmup, 1))
+        # the timed FP64 solves use the mixed arm's seeds (200, 201, ...), so that the last
+        # of each starts from the same vector and their eigenvalues can be compared
+        w64 = min(args.warmup, 1)
+        E64, lat64, pairs64, wall64 = time_arm(p, torch, stream, args.workload, "fp64", fsteps, w64,
+                                               seed0=200 + args.steps - fsteps - w64)
         lam64, X64 = E64.eigenvalues(), E64.eigenvectors()
         stats64 = dict(E64.stats)
 
@@ -536,10 +539,18 @@ def main():
     res = rel_residuals(A, B, lam[:nev], X[:, :nev])
     if lat64:
         res64 = rel_residuals(A, B, lam64[:nev], X64[:, :nev])
+        # The shell's spectrum near the target is a dense cluster, so the two arms (same
+        # start vector, operators equal to ~1e-14) can converge to different subsets of
+        # the nearest eigenvalues; each is checked by its own residual above.  An
+        # eigenvalue that both found agrees to the refinement's accuracy.
         dists = np.array([np.min(np.abs(lam64 - l)) / abs(l) for l in lam[:nev]])
         diff, nmatch = float(dists.max()), int((dists < 1e-10).sum())
+        both = dists[dists < 1e-8]
+        diff_both = float(both.max()) if both.size else None
+        far64 = float(np.max(np.abs(lam64[:nev] - tau)))
+        far = float(np.max(np.abs(lam[:nev] - tau)))
     else:
-        res64, diff, nmatch = np.zeros(1), None, None
+        res64, diff, nmatch, diff_both, far64, far = np.zeros(1), None, None, None, None, None
     stats = dict(E.stats)
     p.close()
 
@@ -583,7 +594,8 @@ def main():
                  if lat64 else None),
         "speedup_vs_fp64": (value / (pairs64 / (sum(lat64) / 1e3))) if lat64 else None,
         "max_eig_resid": float(res.max()), "max_rel_eig_diff_vs_fp64": diff,
-        "eigs_matching_fp64_1e-10": nmatch,
+        "eigs_matching_fp64_1e-10": nmatch, "max_rel_eig_diff_found_by_both": diff_both,
+        "max_dist_to_target": {"mixed": far, "fp64": far64},
         "solver_stats": {k: stats.get(k) for k in ("restarts", "op_applies", "sweeps", "refine_iters_max",
                                                    "solve_resid_max")},
         "gpu_launches": int(launches),
