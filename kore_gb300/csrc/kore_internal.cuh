@@ -32,7 +32,7 @@ struct BcrLevel {
 };
 
 // Rows with more stored values (split A + B) than this are given a whole warp in the
-// sparse products (the dense tau-method boundary rows); the others get 4 lanes.
+// sparse products (the dense tau-method boundary rows); the others get one thread.
 constexpr int kKoreLongRow = 128;
 
 // The pencil is stored l-major and padded: block i (of nblocks K) occupies padded

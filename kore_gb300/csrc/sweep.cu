@@ -517,15 +517,16 @@ __global__ void k_reduce_max(const double *__restrict__ in, int n, double *__res
 }
 
 // Sparse products y = B x, A x - lam B x and the refinement residual b - (A x - lam B x).
-// On this GPU the FP64 pipe, not HBM, bounds them (about one FP64 multiply-add per
+// On this GPU the FP64 pipe, not HBM, bounds them (about two FP64 multiply-adds per
 // SM per clock), so A is stored as a real matrix split into real and imaginary
 // coefficients (two multiply-adds per value instead of four for a complex entry),
 // each row's real and imaginary segments summed separately and combined at the end.
 // Rows are short (a few dozen values): one thread per row with kRowUnroll gathers in
 // flight.  Splitting a row over 2 or 4 lanes costs FP64 additions to combine the
 // partial sums, which take FP64-pipe issue slots like the products do (measured on
-// the 240k-unknown shell: 4 lanes 179 ms, 2 lanes 140 ms, 1 lane 129 ms per solve).  The tau-method boundary rows are dense over a radial expansion
-// (hundreds of entries); rows with more than kKoreLongRow values (A + B) are listed at plan
+// the 240k-unknown shell: 4 lanes 179 ms, 2 lanes 140 ms, 1 lane 129 ms per solve).
+// The tau-method boundary rows are dense over a radial expansion (hundreds of
+// entries); rows with more than kKoreLongRow values (A + B) are listed at plan
 // creation and done by a whole warp each in extra CTAs at the end of the grid, so that
 // they do not hold back the CTAs of the short rows.
 constexpr int kRowLanes = 1;   // threads per short row
