@@ -86,22 +86,22 @@ __device__ __forceinline__ void wait_count(const int *c, int target, int *err) {
 //     A_0, B_0, A_1, B_1, ..., A_{L-1}, B_{L-1}, top, C_{L-1}, ..., C_1, E_0, C_0
 // (A: z_j = D_j^-1 f_j, B: f_i -= L_i z_jl + U_i z_jr, C: x_j = z_j - G_j x_jl - H_j x_jr
 // at levels >= 1; E_0: g_j = c_j - L_j x_jl - U_j x_jr and C_0: x_j = D_j^-1 g_j)
-// and CTA c takes tiles c, c + G, c + 2G, ...  A tile waits only for the counters of
-// the blocks it reads (e.g. a B tile for A of its two neighbours), and after writing
-// its rows it adds 1 to the counter of (stage, block).  Tiles are taken in increasing
+// and CTA c takes tiles c, c + G, c + 2G, ...  A tile reads only blocks whose counters
+// are complete (e.g. a B tile needs A of its two neighbours), and after its rows are
+// written 1 is added to the counter of (stage, block).  Tiles are taken in increasing
 // order by co-resident CTAs, so every wait is on a tile of a lower number that some
 // CTA is processing or has processed: no deadlock, and adjacent stages overlap.
 //
 // A tile of A, C, top or B at levels >= 1 reads one or two S x S blocks (stored
-// column-major); they are cut into
-// chunks of 32 rows x kCols columns (16 KB) that one producer thread copies with
-// cp.async.bulk.tensor into a ring of shared-memory slots, each slot guarded by a
-// "full" mbarrier (completed by the copy) and an "empty" mbarrier (one arrival per
-// consumer warp).  The producer runs ahead through the CTA's tile sequence: the factor
-// data of later tiles does not depend on the sweep, so it is fetched while the eight
-// consumer warps wait for their input vectors.  Several hundred KB per SM are in
-// flight without holding registers.  B_0 and E_0 read the level-0 couplings as padded
-// rows (at most a few dozen entries per row) with plain coalesced loads instead.
+// column-major); they are cut into chunks of 32 rows x kCols columns (16 KB) that one
+// producer thread copies with cp.async.bulk.tensor into a ring of shared-memory slots,
+// each slot guarded by a "full" mbarrier (completed by the copy) and an "empty"
+// mbarrier (one arrival per consumer warp).  The producer runs ahead through the CTA's
+// tile sequence: the factor data of later tiles does not depend on the sweep, so it is
+// fetched while the consumer warps wait for their input vectors.  A dependency-checker
+// warp also runs ahead and publishes in shared memory which tiles have their inputs
+// complete.  B_0 and E_0 read the level-0 couplings as padded rows (at most a few
+// dozen entries per row) with plain coalesced loads instead.
 constexpr int kTmaConsumerWarps = 4;
 constexpr int kTmaConsumers = 32 * kTmaConsumerWarps;
 // CTAs per SM: three CTAs of three or four 16 KB slots keep ~200 KB per SM in flight,
