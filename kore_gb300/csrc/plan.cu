@@ -123,36 +123,40 @@ int permute_csr(const kore_plan *p, const std::vector<int64_t> &orig2slot, const
     val.resize(nnz);
     if (split) split->assign(2 * np, 0);
     int bad = 0;
-#pragma omp parallel for schedule(dynamic, 256) reduction(+ : bad)
-    for (int64_t s = 0; s < np; ++s) {
-        const int64_t o = slot2orig[s];
-        const int64_t blk = s / S;
-        const int b0 = row[s];
-        if (o < 0) {
-            if (split) { (*split)[2 * s] = b0; (*split)[2 * s + 1] = b0; }
-            continue;
+#pragma omp parallel reduction(+ : bad)
+    {
+        std::vector<std::pair<int64_t, int>> tmp;   // one sort buffer per thread
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t s = 0; s < np; ++s) {
+            const int64_t o = slot2orig[s];
+            const int64_t blk = s / S;
+            const int b0 = row[s];
+            if (o < 0) {
+                if (split) { (*split)[2 * s] = b0; (*split)[2 * s + 1] = b0; }
+                continue;
+            }
+            const int e0 = indptr[o], e1 = indptr[o + 1];
+            tmp.resize(e1 - e0);
+            for (int e = e0; e < e1; ++e) {
+                const int64_t c = orig2slot[indices[e]];
+                const int64_t cb = c / S;
+                if (cb < blk - band || cb > blk + band) ++bad;
+                tmp[e - e0] = {c, e};
+            }
+            std::sort(tmp.begin(), tmp.end());
+            int d0 = -1, u0 = -1;
+            for (size_t t = 0; t < tmp.size(); ++t) {
+                col[b0 + t] = (int)tmp[t].first;
+                val[b0 + t] = data[tmp[t].second];
+                const int64_t cb = tmp[t].first / S;
+                if (d0 < 0 && cb >= blk) d0 = b0 + (int)t;
+                if (u0 < 0 && cb >= blk + 1) u0 = b0 + (int)t;
+            }
+            const int end = b0 + (int)tmp.size();
+            if (d0 < 0) d0 = end;
+            if (u0 < 0) u0 = end;
+            if (split) { (*split)[2 * s] = d0; (*split)[2 * s + 1] = u0; }
         }
-        const int e0 = indptr[o], e1 = indptr[o + 1];
-        std::vector<std::pair<int64_t, int>> tmp(e1 - e0);
-        for (int e = e0; e < e1; ++e) {
-            const int64_t c = orig2slot[indices[e]];
-            const int64_t cb = c / S;
-            if (cb < blk - band || cb > blk + band) ++bad;
-            tmp[e - e0] = {c, e};
-        }
-        std::sort(tmp.begin(), tmp.end());
-        int d0 = -1, u0 = -1;
-        for (size_t t = 0; t < tmp.size(); ++t) {
-            col[b0 + t] = (int)tmp[t].first;
-            val[b0 + t] = data[tmp[t].second];
-            const int64_t cb = tmp[t].first / S;
-            if (d0 < 0 && cb >= blk) d0 = b0 + (int)t;
-            if (u0 < 0 && cb >= blk + 1) u0 = b0 + (int)t;
-        }
-        const int end = b0 + (int)tmp.size();
-        if (d0 < 0) d0 = end;
-        if (u0 < 0) u0 = end;
-        if (split) { (*split)[2 * s] = d0; (*split)[2 * s + 1] = u0; }
     }
     return bad ? KORE_EINVAL : KORE_OK;
 }
