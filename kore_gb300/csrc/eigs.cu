@@ -2,7 +2,9 @@
 //
 // Restates what E.solve() does inside SLEPc for bin/solve.py:91-123 with
 // `-st_type sinvert`: Krylov-Schur (Stewart 2001) on OP = (A - tau B)^-1 B.
-//   * Arnoldi expansion with classical Gram-Schmidt applied twice (CGS2) in FP64;
+//   * Arnoldi expansion with classical Gram-Schmidt in FP64 and SLEPc's default
+//     refinement "if needed" (a second pass when the projection removed more than half
+//     of ||w||^2, decided on the device);
 //   * the projected matrix (ncv x ncv) is brought to complex Schur form on the device
 //     (one CTA: Householder reduction to Hessenberg form, single-shift QR sweeps with
 //     Wilkinson shifts and deflation, Givens reordering of the diagonal);
