@@ -1,5 +1,5 @@
 """Batched forced solves: many forcing frequencies sigma = i*omega of one pencil
-factorised and solved in the same kernel launches (SURVEY's batched forced config at
+factorised and solved in the same kernel launches (the tidal-forcing frequency sweep at
 test size), checked against the oracle and against one-at-a-time solves."""
 import numpy as np
 import pytest
