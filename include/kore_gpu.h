@@ -94,8 +94,11 @@ typedef struct {
     int32_t which;        /* KORE_WHICH_* */
     double  target_re, target_im;   /* tau; must equal the factorised shift */
     uint64_t seed;        /* start vector: complex standard normal from this seed */
-    int32_t purify;       /* 1: apply OP once more to each eigenvector (SLEPc default) */
-    double  refine_tol;   /* mixed precision: relative residual of each OP application */
+    int32_t purify;       /* applications of OP to each eigenvector before it is
+                             returned: 1 is SLEPc's default purification, 0 none */
+    double  refine_tol;   /* mixed precision: relative residual of each OP application
+                             (<= 0 selects 1e-15); the purifying application of the
+                             eigenvectors is refined until the residual stops decreasing */
 } kore_eps_opts;
 
 /* Per-call statistics, filled by kore_eigs / kore_solve when the pointer is non-NULL. */
@@ -113,9 +116,10 @@ typedef struct {
 int kore_plan_create(const kore_pencil_desc *desc, int device, kore_plan **plan);
 
 /*
- * Factorises A - sigma B (block Thomas over the l-major blocks, explicit inverses of
- * the diagonal Schur complements, Gauss-Jordan with partial pivoting inside each
- * block).  Replaces the LU that SLEPc's ST sinvert builds inside E.solve()
+ * Factorises A - sigma B (block cyclic reduction over the l-major blocks: explicit
+ * inverses of the eliminated diagonal blocks by Gauss-Jordan with partial pivoting,
+ * their couplings G = D^-1 L, H = D^-1 U, Schur-complement updates of the surviving
+ * blocks, level by level).  Replaces the LU that SLEPc's ST sinvert builds inside E.solve()
  * (bin/solve.py:123) and the KSP preonly+LU factorisation (bin/solve.py:220-227).
  */
 int kore_factor(kore_plan *plan, double sigma_re, double sigma_im, int precision);
@@ -151,13 +155,15 @@ int kore_solve_dev(kore_plan *plan, const void *b_dev, void *x_dev, int nrhs,
  * Its scratch is one file-scope device array of fixed size held by every GPU that
  * loads the library until exit; problems with more than 16384 padded unknowns
  * (blocks x largest block size) are rejected with KORE_EINVAL and a message on
- * stderr.  b_dev and x_dev are complex128 device vectors in the original unknown
- * order; the kernels run on `stream` (0 = the legacy default stream) of the plan's
- * device and the call returns after they finish.  The first call on a device looks
- * up the scratch address (set-up); make that first call before any stream capture.
- * Every call shares the one scratch array and keeps the last call's contents, so
- * calls whose work overlaps on the GPU (other threads, other streams) race: serialise
- * them.
+ * stderr.  The plan must hold one factorised shift (kore_factor); a plan of several
+ * shifts (kore_factor_shifts) is rejected with KORE_EINVAL.  b_dev and x_dev are
+ * complex128 device vectors in the original unknown order; the kernels run on
+ * `stream` (0 = the legacy default stream) of the plan's device, and before returning
+ * the call synchronises that stream and copies the scratch's error and NaN flags to
+ * the host (KORE_ETIMEOUT, KORE_ENAN).  The first call on a device looks up the
+ * scratch address (set-up); make that first call before any stream capture.  Every
+ * call shares the one scratch array and keeps the last call's contents, so calls
+ * whose work overlaps on the GPU (other threads, other streams) race: serialise them.
  */
 int kore_solve_dev_noalloc(kore_plan *plan, const void *b_dev, void *x_dev, double refine_tol,
                            void *stream);
@@ -173,6 +179,26 @@ int kore_solve_dev_noalloc(kore_plan *plan, const void *b_dev, void *x_dev, doub
  */
 int kore_eigs(kore_plan *plan, const kore_eps_opts *opts, double *evals, double *evecs,
               int max_pairs, int *nconv, kore_stats *stats);
+
+/*
+ * Batched form of kore_eigs with continuous admission: ntarget independent
+ * shift-and-invert Krylov-Schur solves on one pencil, run in the plan's nshift
+ * factorised shifts as slots (kore_factor_shifts, nshift <= 32).  Targets 0 .. nshift-1
+ * must be the factorised shifts (opts[t].target = shift t); when a target finishes, the
+ * next one (targets nshift .. ntarget-1) takes its slot: the slot alone is re-factorised
+ * at opts[t].target, in the plan's precision, while the other slots carry on.  Each
+ * target has its own options opts[t] (nev, ncv, tol, maxit, which, seed, purify; the
+ * refinement tolerance of opts[0] applies to all).  The busy slots step together: each
+ * step applies OP once for every busy slot in shared launches (one sparse product and
+ * one sweep over all shifts), and each target's results are those of kore_eigs at that
+ * target.  Target t writes evals + 2 * max_pairs * t, evecs + 2 * n * max_pairs * t (may
+ * be NULL), nconv[t] and stats[t] (may be NULL).  Returns KORE_ENOCONV when a target
+ * converged no pair.  The reference runs one bin/solve.py process per target
+ * (bin/solve.py:91-158, driven over parameter sweeps by tools/dodirs.sh); this replaces
+ * that fan-out.
+ */
+int kore_eigs_shifts(kore_plan *plan, int ntarget, const kore_eps_opts *opts, double *evals, double *evecs,
+                     int max_pairs, int *nconv, kore_stats *stats);
 
 /* y = A x - lambda B x (FP64, original order, host pointers); residual checks. */
 int kore_residual(kore_plan *plan, double lam_re, double lam_im, const double *x, double *y);

@@ -24,7 +24,7 @@ WHICH = {"LM": 0, "SM": 1, "LR": 2, "SR": 3, "LI": 4, "SI": 5, "TM": 6, "TR": 7,
 
 # every function include/kore_gpu.h declares
 EXPORTS = ("kore_plan_create", "kore_factor", "kore_factor_shifts", "kore_solve", "kore_solve_dev",
-           "kore_solve_dev_noalloc", "kore_eigs", "kore_residual", "kore_plan_stream", "kore_profile",
+           "kore_solve_dev_noalloc", "kore_eigs", "kore_eigs_shifts", "kore_residual", "kore_plan_stream", "kore_profile",
            "kore_plan_bytes", "kore_plan_estimate_bytes", "kore_batch_create", "kore_batch_submit",
            "kore_batch_poll", "kore_batch_stats", "kore_batch_destroy", "kore_tc_selftest", "kore_kernel_launches",
            "kore_status_string", "kore_plan_destroy")
@@ -122,6 +122,8 @@ def _bind(lib):
     lib.kore_solve_dev.argtypes = [P, P, P, C.c_int, C.c_double, P, C.POINTER(Stats)]
     lib.kore_solve_dev_noalloc.argtypes = [P, P, P, C.c_double, P]
     lib.kore_eigs.argtypes = [P, C.POINTER(EpsOpts), P, P, C.c_int, C.POINTER(C.c_int), C.POINTER(Stats)]
+    lib.kore_eigs_shifts.argtypes = [P, C.c_int, C.POINTER(EpsOpts), P, P, C.c_int, C.POINTER(C.c_int),
+                                     C.POINTER(Stats)]
     lib.kore_residual.argtypes = [P, C.c_double, C.c_double, P, P]
     lib.kore_plan_stream.argtypes = [P, C.POINTER(P)]
     lib.kore_profile.argtypes = [P, C.c_int, P]

@@ -27,15 +27,13 @@
 namespace {
 
 constexpr int kMaxNcv = 64;
+constexpr int kMaxTargets = 32;   // targets of one batched eigensolve (bits of a mask)
 
 // ----------------------------------------------------------------------------- sort keys
-// Ascending key = wanted first (the comparison functions of SLEPc's `which`).
-__host__ __device__ inline double which_key(double2 theta, int which, double tre, double tim) {
-    // lambda = tau + 1/theta
-    const double d = theta.x * theta.x + theta.y * theta.y;
-    double lre, lim;
-    if (d > 0.0) { lre = tre + theta.x / d; lim = tim - theta.y / d; }
-    else { lre = INFINITY; lim = 0.0; }
+// Ascending key = wanted first (the comparison functions of SLEPc's `which`) of an
+// eigenvalue lambda = (lre, lim) for the target tau = (tre, tim).
+__host__ __device__ inline double lambda_key(double2 lam, int which, double tre, double tim) {
+    const double lre = lam.x, lim = lam.y;
     switch (which) {
         case KORE_WHICH_LM: return -hypot(lre, lim);
         case KORE_WHICH_SM: return hypot(lre, lim);
@@ -49,6 +47,18 @@ __host__ __device__ inline double which_key(double2 theta, int which, double tre
     }
     return 0.0;
 }
+// The same key for a Ritz value theta of OP = (A - tau B)^-1 B: lambda = tau + 1/theta.
+__host__ __device__ inline double which_key(double2 theta, int which, double tre, double tim) {
+    const double d = theta.x * theta.x + theta.y * theta.y;
+    const double2 lam = (d > 0.0) ? mk(tre + theta.x / d, tim - theta.y / d) : mk(INFINITY, 0.0);
+    return lambda_key(lam, which, tre, tim);
+}
+
+// Refinement tolerance that only the FP64 floor stops (the loop ends when the residual
+// no longer decreases): used for the purifying application of the eigenvectors.
+constexpr double kFloorRefineTol = 1e-300;
+// Default relative residual of each OP application inside the Krylov iteration.
+constexpr double kEigsRefineTol = 1e-15;
 
 // ----------------------------------------------------------------------------- small Schur
 struct SchurOut {
@@ -141,12 +151,29 @@ __device__ __forceinline__ void apply_rot(double2 *H, double2 *Q, int m, int k, 
     }
 }
 
-// One CTA of 128 threads (four warps, one per SM sub-partition, so the FP64 updates
-// of a rotation run on all four FP64 pipes).  Hbar: (m+1) x m column-major (ld m+1);
-// row m is the residual row.
+// Per-target parameters of a batched k_schur launch: CTA t works on target t when bit t
+// of `mask` is set; its Hbar, outputs T/Q/Y and theta/est/bnew lie at t times the strides.
+struct SchurBatch {
+    unsigned mask;
+    int m[kMaxTargets], which[kMaxTargets];
+    double tre[kMaxTargets], tim[kMaxTargets];
+    int64_t hstride, sqstride, vstride;
+};
+
+// One CTA of 128 threads per target (four warps, one per SM sub-partition, so the FP64
+// updates of a rotation run on all four FP64 pipes).  Hbar: (m+1) x m column-major
+// (ld m+1); row m is the residual row.
 constexpr int kSchurT = 128;
-__global__ void __launch_bounds__(kSchurT) k_schur(const double2 *__restrict__ Hbar, int m, int which, double tre,
-                                                   double tim, SchurOut out) {
+__global__ void __launch_bounds__(kSchurT) k_schur(const double2 *__restrict__ Hbar0, const SchurBatch sb,
+                                                   SchurOut out0) {
+    const int tg = blockIdx.x;
+    if (!((sb.mask >> tg) & 1u)) return;
+    const int m = sb.m[tg], which = sb.which[tg];
+    const double tre = sb.tre[tg], tim = sb.tim[tg];
+    const double2 *Hbar = Hbar0 + tg * sb.hstride;
+    const SchurOut out{out0.T + tg * sb.sqstride, out0.Q + tg * sb.sqstride, out0.Y + tg * sb.sqstride,
+                       out0.theta + tg * sb.vstride, out0.est + tg * sb.vstride, out0.bnew + tg * sb.vstride,
+                       out0.info + tg};
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2 *H = reinterpret_cast<double2 *>(smem_raw);  // m x m
     double2 *Q = H + m * m;                               // m x m
@@ -340,11 +367,29 @@ __global__ void __launch_bounds__(kSchurT) k_schur(const double2 *__restrict__ H
 }
 
 // ----------------------------------------------------------------------------- tall-skinny kernels
-// partial[b*nc + c] = sum over the CTA's rows of conj(V[:,c]) w for c < ncol, and, with
-// with_norm, entry c = ncol = sum |w|^2 (nc = ncol + with_norm).  run (may be null):
-// the kernel returns at once unless *run != 0.
+// Every kernel below works on all targets of a batched eigensolve at once: grid.y (grid.x
+// for the one-CTA kernels) is the target t, which takes part only when bit t of the
+// launch's mask is set.  Per-target vectors are passed by value as arrays of device
+// pointers, per-target column counts and indices in TCols.
+struct TVec {
+    double2 *p[kMaxTargets];
+};
+struct TCols {
+    unsigned mask;
+    int n[kMaxTargets];     // columns of V the launch uses (rows of G for k_gemm_vg)
+    int j[kMaxTargets];     // column written (Hbar column; output columns for k_gemm_vg)
+    int ld[kMaxTargets];    // leading dimension of the target's Hbar (ncv + 1), or of G
+};
+__device__ __forceinline__ bool in_mask(unsigned mask, int t) { return (mask >> t) & 1u; }
+
 constexpr int kDotThreads = 256;
 constexpr int kDotChunk = 8;
+constexpr int kGridMax = 2048;                                        // CTAs of a tall-skinny kernel
+constexpr int64_t kPartStride = (int64_t)kGridMax * (kMaxNcv + 1);   // per-target CTA partial sums
+constexpr int64_t kHStride = 2 * (kMaxNcv + 1);                      // per-target [h1 | h2]
+constexpr int64_t kHbarStride = (int64_t)(kMaxNcv + 1) * kMaxNcv;
+constexpr int64_t kSqStride = (int64_t)kMaxNcv * kMaxNcv;
+constexpr int64_t kVecStride = kMaxNcv + 1;
 
 // Sums of 16 values over the 32 lanes of a warp with 16 FP64 additions per lane (a
 // butterfly of 5 steps where each lane keeps half of its values and adds the partner's
@@ -363,21 +408,29 @@ __device__ __forceinline__ double warp_transpose_sum16(double (&v)[16], int lane
     }
     return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
 }
-__global__ void __launch_bounds__(kDotThreads) k_mdot(int64_t np, int ncol, const double2 *__restrict__ V,
-                                                      const double2 *__restrict__ w, double2 *__restrict__ partial,
-                                                      int with_norm, const int *__restrict__ run) {
-    if (run && *run == 0) return;
+
+// Target t: partial_t[b*nc + c] = sum over the CTA's rows of conj(V_t[:,c]) w_t for
+// c < ncol_t and, with with_norm, entry c = ncol_t = sum |w_t|^2 (nc = ncol_t + with_norm).
+// run (may be null): target t returns at once unless run[t] != 0.
+__global__ void __launch_bounds__(kDotThreads) k_mdot(int64_t np, TVec V, TVec w, double2 *__restrict__ partial0,
+                                                      int with_norm, const int *__restrict__ run, TCols tc) {
+    const int tg = blockIdx.y;
+    if (!in_mask(tc.mask, tg) || (run && run[tg] == 0)) return;
+    const double2 *__restrict__ Vt = V.p[tg];
+    const double2 *__restrict__ wt = w.p[tg];
+    double2 *__restrict__ partial = partial0 + tg * kPartStride;
     __shared__ double sm[kDotThreads / 32][2 * kDotChunk];
+    const int ncol = tc.n[tg];
     const int nc = ncol + with_norm;
     for (int c0 = 0; c0 < nc; c0 += kDotChunk) {
         double2 acc[kDotChunk];
 #pragma unroll
         for (int t = 0; t < kDotChunk; ++t) acc[t] = mk(0.0, 0.0);
         for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < np; r += (int64_t)gridDim.x * blockDim.x) {
-            const double2 wr = w[r];
+            const double2 wr = wt[r];
 #pragma unroll
             for (int t = 0; t < kDotChunk; ++t)
-                if (c0 + t < nc) acc[t] = cfmaconj(acc[t], (c0 + t < ncol) ? V[r + (int64_t)(c0 + t) * np] : wr, wr);
+                if (c0 + t < nc) acc[t] = cfmaconj(acc[t], (c0 + t < ncol) ? Vt[r + (int64_t)(c0 + t) * np] : wr, wr);
         }
         // warp sums of the 2 kDotChunk doubles: even lane L ends with value L / 2
         double v[2 * kDotChunk];
@@ -397,13 +450,20 @@ __global__ void __launch_bounds__(kDotThreads) k_mdot(int64_t np, int ncol, cons
     }
 }
 
-// h[c] (+)= sum_b partial[b*ncol + c] (one CTA per c); returns at once unless *run != 0
-__global__ void k_mdot_reduce(int nblk, int ncol, const double2 *__restrict__ partial, double2 *__restrict__ h,
-                              int accumulate, const int *__restrict__ run) {
-    if (run && *run == 0) return;
+// Target t (grid.y), column c (grid.x): h_t[c] (+)= sum_b partial_t[b*nc + c] with
+// nc = ncol_t + with_norm; returns at once unless run[t] != 0 (when run is given).
+__global__ void k_mdot_reduce(int nblk, const double2 *__restrict__ partial0, int64_t pstride,
+                              double2 *__restrict__ h0, int accumulate, const int *__restrict__ run, TCols tc,
+                              int with_norm) {
+    const int tg = blockIdx.y;
+    if (!in_mask(tc.mask, tg) || (run && run[tg] == 0)) return;
+    const int nc = tc.n[tg] + with_norm;
     const int c = blockIdx.x;
+    if (c >= nc) return;
+    const double2 *__restrict__ partial = partial0 + tg * pstride;
+    double2 *__restrict__ h = h0 + tg * kHStride;
     double2 s = mk(0.0, 0.0);
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x) s = s + partial[(int64_t)b * ncol + c];
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) s = s + partial[(int64_t)b * nc + c];
     s = warp_sum(s);
     __shared__ double2 sm[32];
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
@@ -415,25 +475,32 @@ __global__ void k_mdot_reduce(int nblk, int ncol, const double2 *__restrict__ pa
     }
 }
 
-// w -= V h  (ncol columns); h is this pass's coefficients; returns at once unless *run != 0
-__global__ void k_mgs_update(int64_t np, int ncol, const double2 *__restrict__ V, const double2 *__restrict__ h,
-                             double2 *__restrict__ w, const int *__restrict__ run) {
-    if (run && *run == 0) return;
+// w_t -= V_t h_t (ncol_t columns); returns at once unless run[t] != 0 (when run is given)
+__global__ void k_mgs_update(int64_t np, TVec V, const double2 *__restrict__ h0, TVec w,
+                             const int *__restrict__ run, TCols tc) {
+    const int tg = blockIdx.y;
+    if (!in_mask(tc.mask, tg) || (run && run[tg] == 0)) return;
+    const double2 *__restrict__ Vt = V.p[tg];
+    double2 *__restrict__ wt = w.p[tg];
+    const int ncol = tc.n[tg];
     __shared__ double2 hs[kMaxNcv + 1];
-    for (int c = threadIdx.x; c < ncol; c += blockDim.x) hs[c] = h[c];
+    for (int c = threadIdx.x; c < ncol; c += blockDim.x) hs[c] = h0[tg * kHStride + c];
     __syncthreads();
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < np; r += (int64_t)gridDim.x * blockDim.x) {
-        double2 acc = w[r];
-        for (int c = 0; c < ncol; ++c) acc = cfms(acc, V[r + (int64_t)c * np], hs[c]);
-        w[r] = acc;
+        double2 acc = wt[r];
+        for (int c = 0; c < ncol; ++c) acc = cfms(acc, Vt[r + (int64_t)c * np], hs[c]);
+        wt[r] = acc;
     }
 }
 
-// partial sums of |w|^2
-__global__ void k_nrm2_partial(int64_t np, const double2 *__restrict__ w, double *__restrict__ partial) {
+// partial_t[b] = sum of |w_t|^2 over CTA b's rows (grid.y = target)
+__global__ void k_nrm2_partial(int64_t np, TVec w, double *__restrict__ partial0, unsigned mask) {
+    const int tg = blockIdx.y;
+    if (!in_mask(mask, tg)) return;
+    const double2 *__restrict__ wt = w.p[tg];
     double s = 0.0;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < np; r += (int64_t)gridDim.x * blockDim.x)
-        s += abs2(w[r]);
+        s += abs2(wt[r]);
     s = warp_sum_d(s);
     __shared__ double sm[32];
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
@@ -441,15 +508,21 @@ __global__ void k_nrm2_partial(int64_t np, const double2 *__restrict__ w, double
     if (threadIdx.x == 0) {
         double t = 0.0;
         for (int wv = 0; wv < (int)(blockDim.x >> 5); ++wv) t += sm[wv];
-        partial[blockIdx.x] = t;
+        partial0[tg * (int64_t)kGridMax + blockIdx.x] = t;
     }
 }
+
 // Refinement decision of classical Gram-Schmidt (SLEPc's default, refinement "if needed"
-// with eta = 1/sqrt(2)): h1[ncol].x = ||w||^2 before the first pass; the norm after it
-// is sqrt(||w||^2 - sum |h1_c|^2) (exact for orthonormal V); a second pass runs when
-// that is below eta ||w||.  Clears h2, which a skipped second pass leaves untouched.
-__global__ void k_refine_decide(const double2 *__restrict__ h1, int ncol, double2 *__restrict__ h2,
-                                int *__restrict__ run2) {
+// with eta = 1/sqrt(2)), one CTA per target: h1[ncol].x = ||w||^2 before the first pass;
+// the norm after it is sqrt(||w||^2 - sum |h1_c|^2) (exact for orthonormal V); a second
+// pass runs when that is below eta ||w||.  Clears h2, which a skipped second pass leaves
+// untouched.
+__global__ void k_refine_decide(double2 *__restrict__ h0, int *__restrict__ run2, TCols tc) {
+    const int tg = blockIdx.x;
+    if (!in_mask(tc.mask, tg)) return;
+    const double2 *__restrict__ h1 = h0 + tg * kHStride;
+    double2 *__restrict__ h2 = h0 + tg * kHStride + (kMaxNcv + 1);
+    const int ncol = tc.n[tg];
     __shared__ double sm[32];
     double s = 0.0;
     for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
@@ -463,48 +536,74 @@ __global__ void k_refine_decide(const double2 *__restrict__ h1, int ncol, double
         double t = 0.0;
         for (int wv = 0; wv < (int)(blockDim.x >> 5); ++wv) t += sm[wv];
         const double onrm2 = h1[ncol].x;
-        *run2 = (onrm2 - t < 0.5 * onrm2) ? 1 : 0;
+        run2[tg] = (onrm2 - t < 0.5 * onrm2) ? 1 : 0;
     }
 }
 
-// beta = sqrt(sum partial); Hbar[j+1 + j*ld] = beta; h (ncol entries) copied into Hbar column j
-__global__ void k_finish_col(int nblk, const double *__restrict__ partial, const double2 *__restrict__ h, int ncol,
-                             double2 *__restrict__ Hbar, int ld, int j, double *__restrict__ beta_out) {
+// One CTA per target: beta_t = sqrt(sum of its partials); with set_col, Hbar_t[j+1, j] =
+// beta_t and h_t (ncol_t entries) becomes column j of Hbar_t (j = tc.j[t], ld tc.ld[t]).
+__global__ void k_finish_col(int nblk, const double *__restrict__ partial0, const double2 *__restrict__ h0,
+                             double2 *__restrict__ Hbar0, double *__restrict__ beta0, TCols tc, int set_col) {
+    const int tg = blockIdx.x;
+    if (!in_mask(tc.mask, tg)) return;
+    const double *__restrict__ partial = partial0 + tg * (int64_t)kGridMax;
     __shared__ double sm[32];
     double s = 0.0;
     for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += partial[b];
     s = warp_sum_d(s);
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
     __syncthreads();
+    double2 *__restrict__ Hbar = Hbar0 + tg * kHbarStride;
+    const int j = tc.j[tg], ld = tc.ld[tg];
     if (threadIdx.x == 0) {
         double t = 0.0;
         for (int wv = 0; wv < (int)(blockDim.x >> 5); ++wv) t += sm[wv];
         const double beta = sqrt(t);
-        *beta_out = beta;
-        if (j >= 0) Hbar[(j + 1) + (int64_t)j * ld] = mk(beta, 0.0);
+        beta0[tg] = beta;
+        if (set_col) Hbar[(j + 1) + (int64_t)j * ld] = mk(beta, 0.0);
     }
-    if (j >= 0)
-        for (int c = threadIdx.x; c < ncol; c += blockDim.x) Hbar[c + (int64_t)j * ld] = h[c];
-}
-// dst = src / *scal (scal > 0), or dst = src * (1/||src||) by passing norm
-__global__ void k_scale_copy(int64_t np, const double2 *__restrict__ src, const double *__restrict__ scal,
-                             double2 *__restrict__ dst) {
-    const double s = *scal;
-    const double inv = (s > 0.0) ? 1.0 / s : 0.0;
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < np; r += (int64_t)gridDim.x * blockDim.x)
-        dst[r] = inv * src[r];
+    if (set_col)
+        for (int c = threadIdx.x; c < tc.n[tg]; c += blockDim.x) Hbar[c + (int64_t)j * ld] = h0[tg * kHStride + c];
 }
 
-// Vout[:, c] = V[:, 0:m] G[:, c] for c < ncol; G is m x ncol column-major (ld m)
+// dst_t = src_t / beta_t (beta_t > 0), else 0; src and dst may be the same vector
+__global__ void k_scale_copy(int64_t np, TVec src, const double *__restrict__ beta0, TVec dst, unsigned mask) {
+    const int tg = blockIdx.y;
+    if (!in_mask(mask, tg)) return;
+    const double s = beta0[tg];
+    const double inv = (s > 0.0) ? 1.0 / s : 0.0;
+    const double2 *__restrict__ a = src.p[tg];
+    double2 *__restrict__ b = dst.p[tg];
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < np; r += (int64_t)gridDim.x * blockDim.x)
+        b[r] = inv * a[r];
+}
+
+// dst_t = src_t (np entries)
+__global__ void k_copy_vecs(int64_t np, TVec src, TVec dst, unsigned mask) {
+    const int tg = blockIdx.y;
+    if (!in_mask(mask, tg)) return;
+    const double2 *__restrict__ a = src.p[tg];
+    double2 *__restrict__ b = dst.p[tg];
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < np; r += (int64_t)gridDim.x * blockDim.x)
+        b[r] = a[r];
+}
+
+// Target t: Vout_t[:, c] = V_t[:, 0:m_t] G_t[:, c] for c < ncol_t, with m_t = tc.n[t],
+// ncol_t = tc.j[t] and G_t column-major with leading dimension tc.ld[t].
 constexpr int kGemmChunk = 8;
-__global__ void k_gemm_vg(int64_t np, int m, int ncol, const double2 *__restrict__ V, const double2 *__restrict__ G,
-                          int ldg, double2 *__restrict__ Vout) {
+__global__ void k_gemm_vg(int64_t np, TVec V, TVec G, TVec Vout, TCols tc) {
+    const int tg = blockIdx.y;
+    if (!in_mask(tc.mask, tg)) return;
+    const int m = tc.n[tg], ncol = tc.j[tg], ldg = tc.ld[tg];
+    const double2 *__restrict__ Vt = V.p[tg];
+    const double2 *__restrict__ Gt = G.p[tg];
+    double2 *__restrict__ Vo = Vout.p[tg];
     __shared__ double2 gs[kMaxNcv * kGemmChunk];
     for (int c0 = 0; c0 < ncol; c0 += kGemmChunk) {
         __syncthreads();
         for (int idx = threadIdx.x; idx < m * kGemmChunk; idx += blockDim.x) {
             const int j = idx % m, t = idx / m;
-            gs[j * kGemmChunk + t] = (c0 + t < ncol) ? G[j + (int64_t)(c0 + t) * ldg] : mk(0.0, 0.0);
+            gs[j * kGemmChunk + t] = (c0 + t < ncol) ? Gt[j + (int64_t)(c0 + t) * ldg] : mk(0.0, 0.0);
         }
         __syncthreads();
         for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < np; r += (int64_t)gridDim.x * blockDim.x) {
@@ -512,21 +611,27 @@ __global__ void k_gemm_vg(int64_t np, int m, int ncol, const double2 *__restrict
 #pragma unroll
             for (int t = 0; t < kGemmChunk; ++t) acc[t] = mk(0.0, 0.0);
             for (int j = 0; j < m; ++j) {
-                const double2 v = V[r + (int64_t)j * np];
+                const double2 v = Vt[r + (int64_t)j * np];
 #pragma unroll
                 for (int t = 0; t < kGemmChunk; ++t) acc[t] = cfma(acc[t], v, gs[j * kGemmChunk + t]);
             }
 #pragma unroll
             for (int t = 0; t < kGemmChunk; ++t)
-                if (c0 + t < ncol) Vout[r + (int64_t)(c0 + t) * np] = acc[t];
+                if (c0 + t < ncol) Vo[r + (int64_t)(c0 + t) * np] = acc[t];
         }
     }
 }
 
-// Hbar <- [T[0:p,0:p]; bnew[0:p]] (ld m+1), other entries zero
-__global__ void k_restart_h(int m, int p, const double2 *__restrict__ T, const double2 *__restrict__ bnew,
-                            double2 *__restrict__ Hbar) {
-    const int ld = m + 1;
+// One CTA per target: Hbar_t <- [T_t[0:p,0:p]; bnew_t[0:p]] (ld m+1), other entries zero,
+// with m = tc.ld[t] - 1 and p = tc.n[t] (the kept Schur vectors)
+__global__ void k_restart_h(const double2 *__restrict__ T0, const double2 *__restrict__ bnew0,
+                            double2 *__restrict__ Hbar0, TCols tc) {
+    const int tg = blockIdx.x;
+    if (!in_mask(tc.mask, tg)) return;
+    const int ld = tc.ld[tg], m = ld - 1, p = tc.n[tg];
+    const double2 *__restrict__ T = T0 + tg * kSqStride;
+    const double2 *__restrict__ bnew = bnew0 + tg * kVecStride;
+    double2 *__restrict__ Hbar = Hbar0 + tg * kHbarStride;
     for (int idx = threadIdx.x; idx < ld * m; idx += blockDim.x) {
         const int r = idx % ld, c = idx / ld;
         double2 v = mk(0.0, 0.0);
@@ -538,17 +643,104 @@ __global__ void k_restart_h(int m, int p, const double2 *__restrict__ T, const d
     }
 }
 
+// Least-squares Rayleigh quotient of an approximate eigenvector x of A x = lambda B x:
+// lambda = (B x)^H (A x) / ||B x||^2 minimises ||A x - lambda B x||_2 over lambda.
+// Target t: partial_t[2 b] = sum conj(bx) ax, partial_t[2 b + 1].x = sum |bx|^2 over
+// CTA b's rows.
+__global__ void k_rq_partial(int64_t np, TVec ax, TVec bx, double2 *__restrict__ partial0, unsigned mask) {
+    const int tg = blockIdx.y;
+    if (!in_mask(mask, tg)) return;
+    const double2 *__restrict__ a = ax.p[tg];
+    const double2 *__restrict__ bv = bx.p[tg];
+    double2 num = mk(0.0, 0.0);
+    double den = 0.0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < np; r += (int64_t)gridDim.x * blockDim.x) {
+        const double2 b = bv[r];
+        num = cfmaconj(num, b, a[r]);
+        den += abs2(b);
+    }
+    num = warp_sum(num);
+    den = warp_sum_d(den);
+    __shared__ double2 sn[32];
+    __shared__ double sd[32];
+    if ((threadIdx.x & 31) == 0) { sn[threadIdx.x >> 5] = num; sd[threadIdx.x >> 5] = den; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { num = num + sn[w]; den += sd[w]; }
+        double2 *partial = partial0 + tg * kPartStride;
+        partial[2 * blockIdx.x] = num;
+        partial[2 * blockIdx.x + 1] = mk(den, 0.0);
+    }
+}
+// One CTA per target: lam_t[k] = sum of numerators / sum of denominators (fixed order)
+__global__ void k_rq_finish(int nblk, const double2 *__restrict__ partial0, double2 *__restrict__ lam0, int k,
+                            unsigned mask) {
+    const int tg = blockIdx.x;
+    if (!in_mask(mask, tg)) return;
+    const double2 *__restrict__ partial = partial0 + tg * kPartStride;
+    double2 num = mk(0.0, 0.0);
+    double den = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) { num = num + partial[2 * b]; den += partial[2 * b + 1].x; }
+    num = warp_sum(num);
+    den = warp_sum_d(den);
+    __shared__ double2 sn[32];
+    __shared__ double sd[32];
+    if ((threadIdx.x & 31) == 0) { sn[threadIdx.x >> 5] = num; sd[threadIdx.x >> 5] = den; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { num = num + sn[w]; den += sd[w]; }
+        lam0[tg * kVecStride + k] = (den > 0.0) ? mk(num.x / den, num.y / den) : mk(NAN, NAN);
+    }
+}
+
+// Clear the refinement statistics of shift s for a new target (the sweep counters,
+// which count launches for the whole plan, are kept).
+__global__ void k_ir_slot_reset(IrState *st, int s) {
+    IrState &x = st[s];
+    x.done = 0; x.nan = 0; x.iters = 0; x.iters_cur = 0; x.iters_max = 0; x.applies = 0;
+    x.prev = 0.0; x.eta_max = 0.0;
+}
+
 // ----------------------------------------------------------------------------- host helpers
+// Device workspace of a batched eigensolve; every per-target array lies at t times its
+// stride.  w, t1 and xin are T x np (target t at t * np).
 struct Ctx {
     kore_plan *p;
+    int T;
     int64_t np;
     unsigned grid;
-    double2 *V, *Vtmp, *w, *t1;
-    double2 *Hbar, *partial, *h;
-    double *dpart, *beta;
-    int *run2;          // second Gram-Schmidt pass needed (device flag)
+    double2 *w, *t1, *xin;
+    double2 *Hbar, *Tm, *Q, *Y, *theta, *bnew, *lam, *h, *partial;
+    double *est, *dpart, *beta;
+    int *info, *run2;
     double refine_tol;
+    std::vector<int> applies;   // applications of OP per target
 };
+
+// bytes of the small per-target arrays (double2 units) of T targets
+size_t small_elems(int T) {
+    const size_t t = (size_t)T;
+    return t * (kHbarStride + 3 * kSqStride + 3 * kVecStride + kHStride + kPartStride) +
+           (t * (kVecStride + kGridMax + 8) + 1) / 2 + (2 * t + 3) / 4 + 4;
+}
+
+void carve_small(Ctx &c, double2 *base) {
+    const int64_t T = c.T;
+    c.Hbar = base;
+    c.Tm = c.Hbar + T * kHbarStride;
+    c.Q = c.Tm + T * kSqStride;
+    c.Y = c.Q + T * kSqStride;
+    c.theta = c.Y + T * kSqStride;
+    c.bnew = c.theta + T * kVecStride;
+    c.lam = c.bnew + T * kVecStride;
+    c.h = c.lam + T * kVecStride;
+    c.partial = c.h + T * kHStride;
+    c.est = reinterpret_cast<double *>(c.partial + T * kPartStride);
+    c.dpart = c.est + T * kVecStride;
+    c.beta = c.dpart + T * kGridMax;
+    c.info = reinterpret_cast<int *>(c.beta + T * 8);
+    c.run2 = c.info + T;
+}
 
 // Deterministic complex standard normal start vector (SplitMix64 + Box-Muller).
 static uint64_t splitmix(uint64_t &s) {
@@ -557,8 +749,7 @@ static uint64_t splitmix(uint64_t &s) {
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     return z ^ (z >> 31);
 }
-static void start_vector(int64_t n, uint64_t seed, std::vector<double2> &v) {
-    v.resize(n);
+static void start_vector(int64_t n, uint64_t seed, double2 *v) {
     uint64_t s = seed;
     const double two_pi = 6.283185307179586476925286766559;
     for (int64_t i = 0; i < n; ++i) {
@@ -569,186 +760,460 @@ static void start_vector(int64_t n, uint64_t seed, std::vector<double2> &v) {
     }
 }
 
-int apply_op(Ctx &c, const double2 *v, double2 *out) {
-    KORE_TRY(kore_spmv_b(c.p, v, c.t1));
-    return kore_apply_inverse(c.p, c.t1, out, c.refine_tol);
+TVec contiguous(double2 *base, int T, int64_t np) {
+    TVec v;
+    for (int t = 0; t < kMaxTargets; ++t) v.p[t] = (t < T) ? base + t * np : nullptr;
+    return v;
 }
 
-// orthogonalise w against V[:, 0:ncol] twice, write h and beta into Hbar column j,
-// v_{j+1} = w / beta
-int orthonormalise(Ctx &c, int ncol, int j, int ldh) {
+// w_t = OP v_t = (A - tau_t B)^-1 B v_t for the targets in mask (one multi-shift sparse
+// product and one multi-shift solve; the other targets' w is left as it is)
+int apply_op(Ctx &c, const TVec &v, unsigned mask, const double *shift_tols = nullptr) {
+    kore_plan *p = c.p;
+    const double2 *x = v.p[0];
+    if (c.T > 1) {
+        k_copy_vecs<<<dim3(c.grid, c.T), 256, 0, p->stream>>>(c.np, v, contiguous(c.xin, c.T, c.np), mask);
+        KORE_LAUNCHED(1);
+        x = c.xin;
+    }
+    KORE_TRY(kore_spmv_b_shifts(p, x, c.t1, mask));
+    for (int t = 0; t < c.T; ++t)
+        if ((mask >> t) & 1u) c.applies[t] += 1;
+    return kore_apply_inverse(p, c.t1, c.w, c.refine_tol, mask, shift_tols);
+}
+
+// For each target t in tc.mask: orthogonalise w_t against V_t[:, 0:ncol_t] (classical
+// Gram-Schmidt with refinement if needed), write h and beta into column j_t of Hbar_t and
+// set V_t[:, j_t + 1] = w_t / beta.
+int orthonormalise(Ctx &c, const TVec &V, const TCols &tc) {
     kore_plan *p = c.p;
     if (p->prof) KORE_TRY(kore_prof_mark(p, 3, true));
+    int nmax = 0;
+    for (int t = 0; t < c.T; ++t)
+        if ((tc.mask >> t) & 1u) nmax = std::max(nmax, tc.n[t]);
+    const TVec w = contiguous(c.w, c.T, c.np);
+    double2 *h1 = c.h, *h2 = c.h + (kMaxNcv + 1);
+    const dim3 g2(c.grid, c.T);
     // first pass, with ||w||^2 as entry ncol of h1
-    double2 *h1 = c.h, *h2 = c.h + kMaxNcv + 1;
-    k_mdot<<<c.grid, kDotThreads, 0, p->stream>>>(c.np, ncol, c.V, c.w, c.partial, 1, nullptr);
-    k_mdot_reduce<<<ncol + 1, 256, 0, p->stream>>>((int)c.grid, ncol + 1, c.partial, h1, 0, nullptr);
-    k_mgs_update<<<c.grid, 256, 0, p->stream>>>(c.np, ncol, c.V, h1, c.w, nullptr);
-    k_refine_decide<<<1, 256, 0, p->stream>>>(h1, ncol, h2, c.run2);
+    k_mdot<<<g2, kDotThreads, 0, p->stream>>>(c.np, V, w, c.partial, 1, nullptr, tc);
+    k_mdot_reduce<<<dim3(nmax + 1, c.T), 256, 0, p->stream>>>((int)c.grid, c.partial, kPartStride, h1, 0, nullptr,
+                                                               tc, 1);
+    k_mgs_update<<<g2, 256, 0, p->stream>>>(c.np, V, h1, w, nullptr, tc);
+    k_refine_decide<<<c.T, 256, 0, p->stream>>>(c.h, c.run2, tc);
     // second pass if needed
-    k_mdot<<<c.grid, kDotThreads, 0, p->stream>>>(c.np, ncol, c.V, c.w, c.partial, 0, c.run2);
-    k_mdot_reduce<<<ncol, 256, 0, p->stream>>>((int)c.grid, ncol, c.partial, h2, 0, c.run2);
-    k_mgs_update<<<c.grid, 256, 0, p->stream>>>(c.np, ncol, c.V, h2, c.w, c.run2);
+    k_mdot<<<g2, kDotThreads, 0, p->stream>>>(c.np, V, w, c.partial, 0, c.run2, tc);
+    k_mdot_reduce<<<dim3(nmax, c.T), 256, 0, p->stream>>>((int)c.grid, c.partial, kPartStride, h2, 0, c.run2, tc, 0);
+    k_mgs_update<<<g2, 256, 0, p->stream>>>(c.np, V, h2, w, c.run2, tc);
     KORE_LAUNCHED(7);
     // h = h1 + h2
-    k_mdot_reduce<<<ncol, 32, 0, p->stream>>>(1, ncol, h2, h1, 1, nullptr);
-    k_nrm2_partial<<<c.grid, 256, 0, p->stream>>>(c.np, c.w, c.dpart);
-    k_finish_col<<<1, 256, 0, p->stream>>>((int)c.grid, c.dpart, c.h, ncol, c.Hbar, ldh, j, c.beta);
-    k_scale_copy<<<c.grid, 256, 0, p->stream>>>(c.np, c.w, c.beta, c.V + (int64_t)(j + 1) * c.np);
+    k_mdot_reduce<<<dim3(nmax, c.T), 32, 0, p->stream>>>(1, h2, kHStride, h1, 1, nullptr, tc, 0);
+    k_nrm2_partial<<<g2, 256, 0, p->stream>>>(c.np, w, c.dpart, tc.mask);
+    k_finish_col<<<c.T, 256, 0, p->stream>>>((int)c.grid, c.dpart, c.h, c.Hbar, c.beta, tc, 1);
+    TVec vnext;
+    for (int t = 0; t < kMaxTargets; ++t)
+        vnext.p[t] = (t < c.T && ((tc.mask >> t) & 1u)) ? V.p[t] + (int64_t)(tc.j[t] + 1) * c.np : nullptr;
+    k_scale_copy<<<g2, 256, 0, p->stream>>>(c.np, w, c.beta, vnext, tc.mask);
     KORE_LAUNCHED(4);
     if (p->prof) KORE_TRY(kore_prof_mark(p, 3, false));
     KORE_CUDA_TRY(cudaGetLastError());
     return KORE_OK;
 }
 
+// One slot of a batched eigensolve: the target it serves and where that target's
+// Krylov-Schur stands.
+struct Slot {
+    int tgt = -1;          // target index (-1: idle)
+    int phase = 2;         // 0 expanding the basis, 1 purifying the eigenvectors, 2 idle
+    int m = 0, nev = 0;    // ncv, nev
+    int j = 0;             // basis vectors formed: the next step writes column j + 1
+    int restarts = 0, nconv = 0, applies = 0;
+    bool failed = false;   // projected problem did not converge
+    double2 *V = nullptr, *Vt = nullptr;   // basis and restart buffers (swapped at restarts)
+    std::vector<double2> theta;            // Ritz values of the last Schur form
+    int nout = 0, k = 0, pstep = 0;        // purification: vectors, next vector, applications done on it
+};
+
+// The state of one kore_eigs_shifts call.
+struct Run {
+    kore_plan *p;
+    Ctx c;
+    int T;                    // slots (= factorised shifts)
+    int ntarget;
+    const kore_eps_opts *o;
+    double *evals, *evecs;
+    int max_pairs;
+    int *nconv_out;
+    kore_stats *st;
+    std::vector<Slot> sl;
+    int next = 0;             // next target to start
+    bool nan = false, none = false;
+    SchurBatch sb{};
+};
+
+// Start target t in slot s: its shift is factorised there unless it is the shift the
+// plan was factorised with (t < T), the basis gets its normalised start vector.
+int start_target(Run &r, int s, int t) {
+    kore_plan *p = r.p;
+    Ctx &c = r.c;
+    const kore_eps_opts &ot = r.o[t];
+    if (t >= r.T) KORE_TRY(kore_factor_slot(p, s, ot.target_re, ot.target_im));
+    Slot &x = r.sl[s];
+    x.tgt = t;
+    x.phase = 0;
+    x.m = ot.ncv > 0 ? ot.ncv : (int)std::min<int64_t>(p->n, std::max(2 * ot.nev, ot.nev + 15));
+    x.nev = ot.nev;
+    x.j = 0; x.restarts = 0; x.nconv = 0; x.applies = 0; x.failed = false;
+    x.nout = 0; x.k = 0; x.pstep = 0;
+    r.sb.m[s] = x.m; r.sb.which[s] = ot.which; r.sb.tre[s] = ot.target_re; r.sb.tim[s] = ot.target_im;
+    // start vector (original order) -> padded -> normalised column 0
+    std::vector<double2> hv((size_t)p->n);
+    start_vector(p->n, ot.seed, hv.data());
+    double2 *orig = c.xin + (int64_t)s * c.np, *pad = c.w + (int64_t)s * c.np;
+    KORE_CUDA_TRY(cudaMemcpyAsync(orig, hv.data(), hv.size() * sizeof(double2), cudaMemcpyHostToDevice, p->stream));
+    KORE_TRY(kore_gather(p, orig, pad));
+    TCols tc{};
+    tc.mask = 1u << s;
+    tc.n[s] = 0; tc.j[s] = -1; tc.ld[s] = x.m + 1;
+    TVec src, dst;
+    for (int u = 0; u < kMaxTargets; ++u) src.p[u] = dst.p[u] = nullptr;
+    src.p[s] = pad; dst.p[s] = x.V;
+    k_nrm2_partial<<<dim3(c.grid, r.T), 256, 0, p->stream>>>(c.np, src, c.dpart, tc.mask);
+    k_finish_col<<<r.T, 256, 0, p->stream>>>((int)c.grid, c.dpart, c.h, c.Hbar, c.beta, tc, 0);
+    k_scale_copy<<<dim3(c.grid, r.T), 256, 0, p->stream>>>(c.np, src, c.beta, dst, tc.mask);
+    k_ir_slot_reset<<<1, 1, 0, p->stream>>>(p->d_ir, s);
+    KORE_LAUNCHED(4);
+    KORE_CUDA_TRY(cudaMemsetAsync(c.Hbar + s * kHbarStride, 0, sizeof(double2) * kHbarStride, p->stream));
+    KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));   // hv is released on return
+    return KORE_OK;
+}
+
+// The target of slot s has its eigenpairs in the device slot arrays: order them by
+// `which`, copy them out, record its statistics, and start the next target if any.
+int finish_target(Run &r, int s) {
+    kore_plan *p = r.p;
+    Ctx &c = r.c;
+    Slot &x = r.sl[s];
+    const int t = x.tgt;
+    const kore_eps_opts &ot = r.o[t];
+    std::vector<double2> lam(std::max(x.nout, 1));
+    IrState irs;
+    if (x.nout > 0)
+        KORE_CUDA_TRY(cudaMemcpyAsync(lam.data(), c.lam + s * kVecStride, x.nout * sizeof(double2),
+                                      cudaMemcpyDeviceToHost, p->stream));
+    KORE_CUDA_TRY(cudaMemcpyAsync(&irs, p->d_ir + s, sizeof(IrState), cudaMemcpyDeviceToHost, p->stream));
+    KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    for (int k = 0; k < x.nout; ++k)
+        if (!(std::isfinite(lam[k].x) && std::isfinite(lam[k].y))) {
+            // B x = 0 or a NaN: keep the back-transformed Ritz value
+            const double2 th = x.theta[k];
+            const double d = th.x * th.x + th.y * th.y;
+            lam[k] = mk(ot.target_re + th.x / d, ot.target_im - th.y / d);
+        }
+    std::vector<int> order(x.nout);
+    std::vector<double> key(x.nout);
+    for (int k = 0; k < x.nout; ++k) {
+        order[k] = k;
+        key[k] = lambda_key(lam[k], ot.which, ot.target_re, ot.target_im);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+    double *ev = r.evals + (size_t)2 * r.max_pairs * t;
+    for (int k = 0; k < x.nout; ++k) {
+        ev[2 * k] = lam[order[k]].x;
+        ev[2 * k + 1] = lam[order[k]].y;
+        if (r.evecs) {
+            KORE_TRY(kore_scatter(p, x.Vt + (int64_t)order[k] * c.np, p->d_v[4]));
+            KORE_CUDA_TRY(cudaMemcpyAsync(r.evecs + ((size_t)r.max_pairs * t + k) * 2 * p->n, p->d_v[4],
+                                          p->n * sizeof(double2), cudaMemcpyDeviceToHost, p->stream));
+        }
+    }
+    KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    r.nconv_out[t] = x.nconv;
+    r.nan = r.nan || irs.nan;
+    r.none = r.none || x.nconv == 0;
+    if (r.st) {
+        kore_stats &q = r.st[t];
+        q.nconv = x.nconv;
+        q.restarts = x.restarts;
+        q.op_applies = x.applies;
+        q.refine_iters_max = irs.iters_max;
+        q.solve_resid_max = irs.eta_max;
+    }
+    x.tgt = -1;
+    x.phase = 2;
+    if (r.next < r.ntarget) return start_target(r, s, r.next++);
+    return KORE_OK;
+}
+
+// Slot s has converged (or run out of restarts): form its Ritz vectors X = V Q Y in the
+// restart buffer and start purifying them (or finish at once without pairs).
+int begin_purify(Run &r, int s, const double2 *theta) {
+    kore_plan *p = r.p;
+    Ctx &c = r.c;
+    Slot &x = r.sl[s];
+    x.theta.assign(theta, theta + x.m);
+    x.nout = std::min(x.nconv, r.max_pairs);
+    if (x.nout == 0) return finish_target(r, s);
+    TCols gc{};
+    gc.mask = 1u << s;
+    gc.n[s] = x.m; gc.j[s] = x.nout; gc.ld[s] = x.m;
+    TVec a, b, d;
+    for (int u = 0; u < kMaxTargets; ++u) a.p[u] = b.p[u] = d.p[u] = nullptr;
+    // G = Q Y[:, 0:nout] (m x nout) into T's storage, then X = V G
+    a.p[s] = c.Q + s * kSqStride; b.p[s] = c.Y + s * kSqStride; d.p[s] = c.Tm + s * kSqStride;
+    k_gemm_vg<<<dim3(1, r.T), 256, 0, p->stream>>>(x.m, a, b, d, gc);
+    a.p[s] = x.V; b.p[s] = c.Tm + s * kSqStride; d.p[s] = x.Vt;
+    k_gemm_vg<<<dim3(c.grid, r.T), 256, 0, p->stream>>>(c.np, a, b, d, gc);
+    KORE_LAUNCHED(2);
+    x.phase = 1;
+    x.k = 0;
+    x.pstep = 0;
+    return KORE_OK;
+}
+
+// Eigenvector k of the slots in mask is final (purified): normalise it and take its
+// eigenvalue as the FP64 least-squares Rayleigh quotient (B x)^H (A x) / ||B x||^2.
+int finish_vectors(Run &r, const TVec &x, unsigned mask, const int *kidx) {
+    kore_plan *p = r.p;
+    Ctx &c = r.c;
+    const int64_t np = c.np;
+    TCols nc{};
+    nc.mask = mask;
+    k_nrm2_partial<<<dim3(c.grid, r.T), 256, 0, p->stream>>>(np, x, c.dpart, mask);
+    k_finish_col<<<r.T, 256, 0, p->stream>>>((int)c.grid, c.dpart, c.h, c.Hbar, c.beta, nc, 0);
+    k_scale_copy<<<dim3(c.grid, r.T), 256, 0, p->stream>>>(np, x, c.beta, x, mask);
+    k_copy_vecs<<<dim3(c.grid, r.T), 256, 0, p->stream>>>(np, x, contiguous(c.xin, r.T, np), mask);
+    KORE_LAUNCHED(4);
+    KORE_TRY(kore_spmv_a_shifts(p, c.xin, c.w, mask));
+    KORE_TRY(kore_spmv_b_shifts(p, c.xin, c.t1, mask));
+    k_rq_partial<<<dim3(c.grid, r.T), 256, 0, p->stream>>>(np, contiguous(c.w, r.T, np), contiguous(c.t1, r.T, np),
+                                                          c.partial, mask);
+    KORE_LAUNCHED(1);
+    // k differs between slots: one finishing launch per distinct k
+    unsigned left = mask;
+    while (left) {
+        const int s0 = __builtin_ctz(left);
+        unsigned same = 0;
+        for (int s = 0; s < r.T; ++s)
+            if (((left >> s) & 1u) && kidx[s] == kidx[s0]) same |= 1u << s;
+        k_rq_finish<<<r.T, 256, 0, p->stream>>>((int)c.grid, c.partial, c.lam, kidx[s0], same);
+        KORE_LAUNCHED(1);
+        left &= ~same;
+    }
+    return KORE_OK;
+}
+
 }  // namespace
 
-int kore_eigs_impl(kore_plan *p, const kore_eps_opts *o, double *evals, double *evecs, int max_pairs, int *nconv_out,
-                   kore_stats *st) {
+// Batched shift-and-invert Krylov-Schur with continuous admission.  The plan's nshift
+// factorised shifts are slots; targets 0 .. nshift-1 start in them, and when a target
+// finishes, the next target (ntarget >= nshift) takes its slot: the slot's shift is
+// re-factorised and a new basis started while the other slots carry on.  Target t runs
+// its own Krylov-Schur with options o[t].  One step applies OP once for every busy slot
+// in shared launches (one multi-shift sparse product and one multi-shift sweep plus the
+// FP64 refinement loop in mixed precision): an expanding slot extends its Arnoldi basis
+// (batched Gram-Schmidt kernels follow), a purifying slot applies OP to its next Ritz
+// vector.  A slot whose basis is full gets its projected Schur problem (one CTA per such
+// slot), its convergence test and its thick restart independently of the others.
+int kore_eigs_impl(kore_plan *p, int ntarget, const kore_eps_opts *o, double *evals, double *evecs, int max_pairs,
+                   int *nconv_out, kore_stats *st) {
     if (!p->factored) return KORE_ENOTFACTORED;
-    if (!p->has_b || !o || o->nev <= 0 || o->which < 0 || o->which > 8) return KORE_EINVAL;
-    if (o->target_re != p->sigma_re || o->target_im != p->sigma_im) return KORE_EINVAL;
+    const int T = p->nshift;
+    if (!p->has_b || !o || T < 1 || T > kMaxTargets || ntarget < T) return KORE_EINVAL;
     const int64_t n = p->n, np = p->np;
-    const int nev = o->nev;
-    int m = o->ncv > 0 ? o->ncv : (int)std::min<int64_t>(n, std::max(2 * nev, nev + 15));
-    if (m > kMaxNcv || m <= nev || m > n) return KORE_EINVAL;
+    int M = 0;
+    for (int t = 0; t < ntarget; ++t) {
+        const kore_eps_opts &ot = o[t];
+        if (ot.nev <= 0 || ot.which < 0 || ot.which > 8 || ot.purify < 0) return KORE_EINVAL;
+        if (t < T && (ot.target_re != p->sigmas[t].x || ot.target_im != p->sigmas[t].y)) return KORE_EINVAL;
+        const int m = ot.ncv > 0 ? ot.ncv : (int)std::min<int64_t>(n, std::max(2 * ot.nev, ot.nev + 15));
+        if (m > kMaxNcv || m <= ot.nev || m > n) return KORE_EINVAL;
+        M = std::max(M, m);
+    }
     auto t0 = std::chrono::steady_clock::now();
-    if (st) *st = kore_stats{};
+    if (st)
+        for (int t = 0; t < ntarget; ++t) st[t] = kore_stats{};
 
-    // workspace
-    if (p->ks_cap < m + 1) {
-        cudaFree(p->d_V); cudaFree(p->d_Vtmp);
-        p->d_V = p->d_Vtmp = nullptr;
-        KORE_TRY(kore_alloc(p, (void **)&p->d_V, (size_t)np * (m + 1) * sizeof(double2)));
-        KORE_TRY(kore_alloc(p, (void **)&p->d_Vtmp, (size_t)np * (m + 1) * sizeof(double2)));
-        p->ks_cap = m + 1;
+    // workspace: per slot a basis and a restart buffer of M + 1 columns
+    const int64_t vcols = (int64_t)T * (M + 1);
+    if (p->ks_cap < vcols) {
+        cudaFree(p->d_V); cudaFree(p->d_Vtmp); cudaFree(p->d_ksx);
+        p->d_V = p->d_Vtmp = p->d_ksx = nullptr;
+        p->ks_cap = 0;
+        KORE_TRY(kore_alloc(p, (void **)&p->d_V, (size_t)np * vcols * sizeof(double2)));
+        KORE_TRY(kore_alloc(p, (void **)&p->d_Vtmp, (size_t)np * vcols * sizeof(double2)));
+        KORE_TRY(kore_alloc(p, (void **)&p->d_ksx, (size_t)np * T * sizeof(double2)));
+        p->ks_cap = vcols;
     }
-    if (!p->d_small) {
-        // Hbar, T, Q, Y, theta, est, bnew, h(2x), partial, dpart, beta, info
-        const size_t sz = (size_t)(kMaxNcv + 1) * kMaxNcv * 4 + 8 * (kMaxNcv + 1) + 2048 * (kMaxNcv + 1) + 4096;
-        KORE_TRY(kore_alloc(p, (void **)&p->d_small, sz * sizeof(double2)));
+    if (p->ks_small_cap < T) {
+        cudaFree(p->d_small);
+        p->d_small = nullptr;
+        p->ks_small_cap = 0;
+        KORE_TRY(kore_alloc(p, (void **)&p->d_small, small_elems(T) * sizeof(double2)));
+        p->ks_small_cap = T;
     }
-    double2 *base = p->d_small;
-    const int ldh = m + 1;
-    Ctx c;
-    c.p = p; c.np = np;
+    Run r;
+    r.p = p; r.T = T; r.ntarget = ntarget; r.o = o; r.evals = evals; r.evecs = evecs; r.max_pairs = max_pairs;
+    r.nconv_out = nconv_out; r.st = st;
+    Ctx &c = r.c;
+    c.p = p; c.T = T; c.np = np;
     c.grid = std::min<unsigned>(kore_div_up(np, 256), 2u * p->num_sms);
-    c.V = p->d_V; c.Vtmp = p->d_Vtmp; c.w = p->d_v[2]; c.t1 = p->d_v[3];
-    c.Hbar = base;
-    double2 *dT = base + (kMaxNcv + 1) * kMaxNcv;
-    double2 *dQ = dT + kMaxNcv * kMaxNcv;
-    double2 *dY = dQ + kMaxNcv * kMaxNcv;
-    double2 *dtheta = dY + kMaxNcv * kMaxNcv;
-    double2 *dbnew = dtheta + (kMaxNcv + 1);
-    c.h = dbnew + (kMaxNcv + 1);                    // 2 x (kMaxNcv+1)
-    double *dest = reinterpret_cast<double *>(c.h + 2 * (kMaxNcv + 1));   // kMaxNcv+1 doubles
-    c.partial = c.h + 3 * (kMaxNcv + 1);             // grid x ncol
-    c.dpart = reinterpret_cast<double *>(c.partial + 2048 * (kMaxNcv + 1));
-    c.beta = c.dpart + 2048;
-    int *dinfo = reinterpret_cast<int *>(c.beta + 8);
-    c.run2 = dinfo + 4;
-    if (c.grid > 2048) return KORE_EINVAL;
-
-    // start vector
-    std::vector<double2> hv;
-    start_vector(n, o->seed, hv);
-    KORE_CUDA_TRY(cudaMemcpyAsync(p->d_v[4], hv.data(), n * sizeof(double2), cudaMemcpyHostToDevice, p->stream));
-    KORE_TRY(kore_gather(p, p->d_v[4], c.w));
-    k_nrm2_partial<<<c.grid, 256, 0, p->stream>>>(np, c.w, c.dpart);
-    k_finish_col<<<1, 256, 0, p->stream>>>((int)c.grid, c.dpart, c.h, 0, c.Hbar, ldh, -1, c.beta);
-    k_scale_copy<<<c.grid, 256, 0, p->stream>>>(np, c.w, c.beta, c.V);
-    KORE_LAUNCHED(3);
-    KORE_CUDA_TRY(cudaMemsetAsync(c.Hbar, 0, sizeof(double2) * ldh * m, p->stream));
-
-    const size_t schur_smem = (size_t)3 * m * m * sizeof(double2);
-    KORE_TRY(kore_allow_max_dyn_smem(k_schur, p->device));
-    std::vector<double> h_est(m);
-    std::vector<double2> h_theta(m);
-    int h_info = 0;
-    int kkeep = 0, nconv = 0, restarts = 0;
-    c.refine_tol = o->refine_tol;
+    if (c.grid > (unsigned)kGridMax) return KORE_EINVAL;
+    c.t1 = p->d_bb; c.w = p->d_xb; c.xin = p->d_ksx;
+    carve_small(c, p->d_small);
+    c.applies.assign(T, 0);
+    // Each OP application of an expanding slot is refined to 1e-15 unless asked
+    // otherwise: at 1e-14 the eigen residuals of the mixed path were ten times the FP64
+    // path's on the 240k shell and ill-conditioned eigenvalues drifted further than a
+    // rounding-level perturbation of A moves them; at 1e-15 both match the FP64 path.
+    // A purifying application is refined until its residual stops decreasing, so a
+    // returned vector carries no more of the complex64 factors' error than necessary.
+    c.refine_tol = (o[0].refine_tol > 0.0) ? o[0].refine_tol : kEigsRefineTol;
+    r.sl.assign(T, Slot{});
+    for (int s = 0; s < T; ++s) {
+        r.sl[s].V = p->d_V + (int64_t)s * (M + 1) * np;
+        r.sl[s].Vt = p->d_Vtmp + (int64_t)s * (M + 1) * np;
+    }
     KORE_TRY(kore_ir_reset(p));
-    for (restarts = 0;; ++restarts) {
-        // Arnoldi expansion kkeep .. m-1
-        for (int j = kkeep; j < m; ++j) {
-            KORE_TRY(apply_op(c, c.V + (int64_t)j * np, c.w));
-            KORE_TRY(orthonormalise(c, j + 1, j, ldh));
+    KORE_TRY(kore_allow_max_dyn_smem(k_schur, p->device));
+    const size_t schur_smem = (size_t)3 * M * M * sizeof(double2);
+    r.sb.hstride = kHbarStride; r.sb.sqstride = kSqStride; r.sb.vstride = kVecStride;
+    const SchurOut so{c.Tm, c.Q, c.Y, c.theta, c.est, c.bnew, c.info};
+    for (int s = 0; s < T; ++s) KORE_TRY(start_target(r, s, s));
+    r.next = T;
+    std::vector<double> h_est((size_t)T * kVecStride);
+    std::vector<double2> h_theta((size_t)T * kVecStride);
+    std::vector<int> h_info(T);
+    std::vector<double> tols(T);
+    std::vector<int> kidx(T);
+    const bool mixed = p->prec == KORE_PREC_MIXED;
+
+    for (;;) {
+        unsigned expm = 0, purm = 0;
+        for (int s = 0; s < T; ++s) {
+            if (r.sl[s].phase == 0) expm |= 1u << s;
+            else if (r.sl[s].phase == 1) purm |= 1u << s;
         }
+        if (!(expm | purm)) break;
+        // one application of OP for every busy slot
+        TVec vin, vb;
+        TCols tc{};
+        tc.mask = expm;
+        for (int u = 0; u < kMaxTargets; ++u) vin.p[u] = vb.p[u] = nullptr;
+        for (int s = 0; s < T; ++s) {
+            Slot &x = r.sl[s];
+            vb.p[s] = x.V;
+            vin.p[s] = (x.phase == 1) ? x.Vt + (int64_t)x.k * np : x.V + (int64_t)x.j * np;
+            tc.n[s] = x.j + 1; tc.j[s] = x.j; tc.ld[s] = x.m + 1;
+            tols[s] = (x.phase == 1 && mixed) ? kFloorRefineTol : c.refine_tol;
+            kidx[s] = x.k;
+        }
+        // a purifying slot with purify = 0 skips the application
+        unsigned appm = expm;
+        for (int s = 0; s < T; ++s)
+            if (((purm >> s) & 1u) && r.o[r.sl[s].tgt].purify > 0) appm |= 1u << s;
+        if (appm) KORE_TRY(apply_op(c, vin, appm, tols.data()));
+        for (int s = 0; s < T; ++s)
+            if ((appm >> s) & 1u) r.sl[s].applies += 1;
+        if (expm) KORE_TRY(orthonormalise(c, vb, tc));
+        if (purm) {
+            // x <- OP x for the purifying slots that applied it; a vector is final after
+            // opts.purify applications
+            unsigned app_p = appm & purm, fin = 0;
+            k_copy_vecs<<<dim3(c.grid, T), 256, 0, p->stream>>>(np, contiguous(c.w, T, np), vin, app_p);
+            KORE_LAUNCHED(1);
+            for (int s = 0; s < T; ++s)
+                if ((purm >> s) & 1u) {
+                    Slot &x = r.sl[s];
+                    if ((app_p >> s) & 1u) x.pstep += 1;
+                    if (x.pstep >= r.o[x.tgt].purify) fin |= 1u << s;
+                }
+            if (fin) KORE_TRY(finish_vectors(r, vin, fin, kidx.data()));
+            for (int s = 0; s < T; ++s)
+                if ((fin >> s) & 1u) {
+                    Slot &x = r.sl[s];
+                    x.k += 1;
+                    x.pstep = 0;
+                    if (x.k == x.nout) KORE_TRY(finish_target(r, s));
+                }
+        }
+        unsigned full = 0;
+        for (int s = 0; s < T; ++s)
+            if ((expm >> s) & 1u) {
+                r.sl[s].j += 1;
+                if (r.sl[s].j == r.sl[s].m) full |= 1u << s;
+            }
+        if (!full) continue;
+        // projected Schur problems of the slots whose basis is full
         if (p->prof) KORE_TRY(kore_prof_mark(p, 4, true));
-        SchurOut so{dT, dQ, dY, dtheta, dest, dbnew, dinfo};
-        k_schur<<<1, kSchurT, schur_smem, p->stream>>>(c.Hbar, m, o->which, o->target_re, o->target_im, so);
+        r.sb.mask = full;
+        k_schur<<<T, kSchurT, schur_smem, p->stream>>>(c.Hbar, r.sb, so);
         KORE_LAUNCHED(1);
         KORE_CUDA_TRY(cudaGetLastError());
         if (p->prof) KORE_TRY(kore_prof_mark(p, 4, false));
-        KORE_CUDA_TRY(cudaMemcpyAsync(h_est.data(), dest, m * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
-        KORE_CUDA_TRY(cudaMemcpyAsync(h_theta.data(), dtheta, m * sizeof(double2), cudaMemcpyDeviceToHost, p->stream));
-        KORE_CUDA_TRY(cudaMemcpyAsync(&h_info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+        KORE_CUDA_TRY(cudaMemcpyAsync(h_est.data(), c.est, h_est.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                      p->stream));
+        KORE_CUDA_TRY(cudaMemcpyAsync(h_theta.data(), c.theta, h_theta.size() * sizeof(double2),
+                                      cudaMemcpyDeviceToHost, p->stream));
+        KORE_CUDA_TRY(cudaMemcpyAsync(h_info.data(), c.info, T * sizeof(int), cudaMemcpyDeviceToHost, p->stream));
         KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
         KORE_TRY(kore_check_device_error(p));
-        if (h_info != 0) return KORE_ENOCONV;
-        nconv = 0;
-        while (nconv < m && h_est[nconv] < o->tol) ++nconv;
-        if (nconv >= nev || restarts + 1 >= o->maxit) break;
-        // thick restart
-        const int l = std::max(1, (m - nconv) / 2);
-        const int keep = std::min(nconv + l, m - 1);
-        if (p->prof) KORE_TRY(kore_prof_mark(p, 4, true));
-        k_gemm_vg<<<c.grid, 256, 0, p->stream>>>(np, m, keep, c.V, dQ, m, c.Vtmp);
-        KORE_CUDA_TRY(cudaMemcpyAsync(c.Vtmp + (int64_t)keep * np, c.V + (int64_t)m * np, np * sizeof(double2),
-                                      cudaMemcpyDeviceToDevice, p->stream));
-        k_restart_h<<<1, 256, 0, p->stream>>>(m, keep, dT, dbnew, c.Hbar);
-        KORE_LAUNCHED(2);
-        if (p->prof) KORE_TRY(kore_prof_mark(p, 4, false));
-        std::swap(c.V, c.Vtmp);
-        kkeep = keep;
-    }
-    // keep the plan's pointers consistent with the swapped buffers
-    p->d_V = c.V;
-    p->d_Vtmp = c.Vtmp;
-    const int nout = std::min(nconv, max_pairs);
-    // eigenvalues in Schur order (already sorted by `which`)
-    for (int j = 0; j < nout; ++j) {
-        const double2 th = h_theta[j];
-        const double d = th.x * th.x + th.y * th.y;
-        evals[2 * j] = o->target_re + th.x / d;
-        evals[2 * j + 1] = o->target_im - th.y / d;
-    }
-    if (evecs && nout > 0) {
-        // Ritz vectors X = V Q Y[:, 0:nout]: G = Q Y (m x nout) on the device, then V G
-        // G computed column by column with the tall-skinny kernel on the small matrices
-        double2 *G = dT;  // reuse T storage: m x nout
-        k_gemm_vg<<<1, 256, 0, p->stream>>>(m, m, nout, dQ, dY, m, G);
-        k_gemm_vg<<<c.grid, 256, 0, p->stream>>>(np, m, nout, c.V, G, m, c.Vtmp);
-        KORE_LAUNCHED(2);
-        for (int j = 0; j < nout; ++j) {
-            double2 *x = c.Vtmp + (int64_t)j * np;
-            if (o->purify) {
-                KORE_TRY(apply_op(c, x, c.w));
-                KORE_CUDA_TRY(cudaMemcpyAsync(x, c.w, np * sizeof(double2), cudaMemcpyDeviceToDevice, p->stream));
+        // convergence tests and thick restarts
+        TCols rc{};
+        TVec rV, rQ, rOut, rSrc, rDst;
+        for (int u = 0; u < kMaxTargets; ++u) rV.p[u] = rQ.p[u] = rOut.p[u] = rSrc.p[u] = rDst.p[u] = nullptr;
+        for (int s = 0; s < T; ++s) {
+            if (!((full >> s) & 1u)) continue;
+            Slot &x = r.sl[s];
+            const kore_eps_opts &ot = r.o[x.tgt];
+            x.restarts += 1;
+            if (h_info[s] != 0) {
+                x.failed = true;
+                x.nconv = 0;
+                KORE_TRY(begin_purify(r, s, h_theta.data() + (size_t)s * kVecStride));
+                continue;
             }
-            k_nrm2_partial<<<c.grid, 256, 0, p->stream>>>(np, x, c.dpart);
-            k_finish_col<<<1, 256, 0, p->stream>>>((int)c.grid, c.dpart, c.h, 0, c.Hbar, ldh, -1, c.beta);
-            k_scale_copy<<<c.grid, 256, 0, p->stream>>>(np, x, c.beta, c.w);
+            const double *est = h_est.data() + (size_t)s * kVecStride;
+            int ncv = 0;
+            while (ncv < x.m && est[ncv] < ot.tol) ++ncv;
+            x.nconv = ncv;
+            if (ncv >= x.nev || x.restarts >= ot.maxit) {
+                KORE_TRY(begin_purify(r, s, h_theta.data() + (size_t)s * kVecStride));
+                continue;
+            }
+            const int l = std::max(1, (x.m - ncv) / 2);
+            const int keep = std::min(ncv + l, x.m - 1);
+            rc.mask |= 1u << s;
+            rc.n[s] = x.m; rc.j[s] = keep; rc.ld[s] = x.m;
+            rV.p[s] = x.V; rQ.p[s] = c.Q + s * kSqStride; rOut.p[s] = x.Vt;
+            rSrc.p[s] = x.V + (int64_t)x.m * np; rDst.p[s] = x.Vt + (int64_t)keep * np;
+        }
+        if (rc.mask) {
+            if (p->prof) KORE_TRY(kore_prof_mark(p, 4, true));
+            k_gemm_vg<<<dim3(c.grid, T), 256, 0, p->stream>>>(np, rV, rQ, rOut, rc);
+            k_copy_vecs<<<dim3(c.grid, T), 256, 0, p->stream>>>(np, rSrc, rDst, rc.mask);
+            TCols hc = rc;
+            for (int s = 0; s < T; ++s) { hc.n[s] = rc.j[s]; hc.ld[s] = r.sl[s].m + 1; }
+            k_restart_h<<<T, 256, 0, p->stream>>>(c.Tm, c.bnew, c.Hbar, hc);
             KORE_LAUNCHED(3);
-            KORE_TRY(kore_scatter(p, c.w, p->d_v[4]));
-            KORE_CUDA_TRY(cudaMemcpyAsync(evecs + 2 * n * (int64_t)j, p->d_v[4], n * sizeof(double2),
-                                          cudaMemcpyDeviceToHost, p->stream));
+            if (p->prof) KORE_TRY(kore_prof_mark(p, 4, false));
+            for (int s = 0; s < T; ++s)
+                if ((rc.mask >> s) & 1u) {
+                    std::swap(r.sl[s].V, r.sl[s].Vt);
+                    r.sl[s].j = rc.j[s];
+                }
         }
     }
     KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
     KORE_TRY(kore_check_device_error(p));
-    *nconv_out = nconv;
-    IrState irs;
-    KORE_TRY(kore_ir_read(p, &irs));
-    if (irs.nan) return KORE_ENAN;
-    if (st) {
-        st->nconv = nconv;
-        st->restarts = restarts + 1;
-        st->op_applies = (p->prec == KORE_PREC_MIXED) ? irs.applies : irs.sweeps;
-        st->sweeps = irs.sweeps;
-        st->refine_iters_max = irs.iters_max;
-        st->solve_resid_max = irs.eta_max;
-        st->iterate_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    }
-    return nconv > 0 ? KORE_OK : KORE_ENOCONV;
+    IrState ir0;
+    KORE_CUDA_TRY(cudaMemcpyAsync(&ir0, p->d_ir, sizeof(IrState), cudaMemcpyDeviceToHost, p->stream));
+    KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (st)
+        for (int t = 0; t < ntarget; ++t) {
+            st[t].sweeps = ir0.sweeps;   // every sweep launch counts in shift 0's state
+            st[t].iterate_ms = ms;
+        }
+    if (r.nan) return KORE_ENAN;
+    return r.none ? KORE_ENOCONV : KORE_OK;
 }

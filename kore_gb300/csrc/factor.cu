@@ -62,18 +62,24 @@ struct FV {
     int64_t f_stride, lu_stride, t_stride, p_stride;
 };
 
+// View of the plan's factor storage starting at the factor window's first shift (shift
+// fw_lo + s of the plan is shift s of the view).
 template <typename C>
 FV<C> make_fv(kore_plan *p) {
     FV<C> v;
+    const int64_t lo = p->fw_lo;
     v.S = p->S; v.K = p->K; v.np = p->np;
     v.arow = p->d_arow; v.acol = p->d_acol; v.asplit = p->d_asplit; v.brow = p->d_brow; v.bcol = p->d_bcol;
     v.bsz = p->d_bsz; v.aval = p->d_aval; v.bval = p->d_bval; v.has_b = p->has_b ? 1 : 0;
-    v.sigma = p->d_sigma; v.rscale = p->d_rscale;
-    v.Dinv = static_cast<C *>(p->d_Dinv); v.G = static_cast<C *>(p->d_Gm); v.H = static_cast<C *>(p->d_Hm);
-    v.Dw = static_cast<C *>(p->d_Dw); v.LU = static_cast<C *>(p->d_LU); v.T = static_cast<C *>(p->d_T);
-    v.piv = p->d_piv; v.pidx = p->d_pidx; v.used = p->d_used; v.err = p->d_err;
+    v.sigma = p->d_sigma + lo; v.rscale = p->d_rscale + lo * p->np;
+    v.Dinv = static_cast<C *>(p->d_Dinv) + lo * p->f_stride(); v.G = static_cast<C *>(p->d_Gm) + lo * p->f_stride();
+    v.H = static_cast<C *>(p->d_Hm) + lo * p->f_stride(); v.Dw = static_cast<C *>(p->d_Dw) + lo * p->f_stride();
+    v.LU = static_cast<C *>(p->d_LU) + lo * p->lu_stride(); v.T = static_cast<C *>(p->d_T) + lo * p->t_stride();
+    v.piv = p->d_piv + lo * p->p_stride(); v.pidx = p->d_pidx + lo * p->p_stride();
+    v.used = p->d_used + lo * p->p_stride(); v.err = p->d_err;
     v.cc_ptr = p->d_cc_ptr; v.cc_row = p->d_cc_row; v.cc_src = p->d_cc_src;
-    v.ell_col = p->d_ell_col; v.ell_val = static_cast<const C *>(p->d_ell_val); v.ell_w = p->ell_w;
+    v.ell_col = p->d_ell_col; v.ell_val = static_cast<const C *>(p->d_ell_val) + lo * p->ell_stride();
+    v.ell_w = p->ell_w;
     v.ell_stride = p->ell_stride();
     v.f_stride = p->f_stride(); v.lu_stride = p->lu_stride(); v.t_stride = p->t_stride(); v.p_stride = p->p_stride();
     return v;
@@ -607,7 +613,7 @@ int gauss_jordan(kore_plan *p, const FV<C> &v, const BcrLevel &lv, int nodd, int
 
 template <typename C, int NB>
 int factor_levels(kore_plan *p) {
-    const int S = p->S, K = p->K, ns = p->nshift;
+    const int S = p->S, K = p->K, ns = p->fw_n;
     const int64_t SS = (int64_t)S * S;
     cudaStream_t st = p->stream;
     const FV<C> v = make_fv<C>(p);
@@ -780,6 +786,8 @@ int kore_factor_impl(kore_plan *p, int nshift, const double *sigmas, int precisi
     KORE_TRY(ensure_factor_storage(p, nshift, elt));
     p->prec = precision;
     p->nshift = nshift;
+    p->fw_lo = 0;
+    p->fw_n = nshift;
     p->sigmas.assign(nshift, mk(0.0, 0.0));
     for (int s = 0; s < nshift; ++s) p->sigmas[s] = mk(sigmas[2 * s], sigmas[2 * s + 1]);
     p->sigma_re = sigmas[0];
@@ -819,6 +827,61 @@ int kore_factor_impl(kore_plan *p, int nshift, const double *sigmas, int precisi
         for (unsigned b = 0; b < grid; ++b) p->minfs[sh] = std::max(p->minfs[sh], red[(size_t)sh * grid + b]);
     p->minf = p->minfs[0];
     KORE_CUDA_TRY(cudaMemcpyAsync(p->d_minf, p->minfs.data(), nshift * sizeof(double), cudaMemcpyHostToDevice,
+                                  p->stream));
+    KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    KORE_TRY(kore_check_device_error(p));
+    p->factored = true;
+    return KORE_OK;
+}
+
+// Re-factorise one shift of a factorised plan: shift `slot` becomes A - sigma B and the
+// other shifts keep their factors (the factor window is narrowed to the slot for the
+// launches).  A batched eigensolve uses it to start a new target in a slot whose target
+// has finished while the other slots carry on.
+int kore_factor_slot(kore_plan *p, int slot, double sigma_re, double sigma_im) {
+    if (!p->factored || slot < 0 || slot >= p->nshift) return KORE_EINVAL;
+    p->factored = false;
+    p->sigmas[slot] = mk(sigma_re, sigma_im);
+    if (slot == 0) { p->sigma_re = sigma_re; p->sigma_im = sigma_im; }
+    KORE_CUDA_TRY(cudaMemcpyAsync(p->d_sigma + slot, &p->sigmas[slot], sizeof(double2), cudaMemcpyHostToDevice,
+                                  p->stream));
+    p->fw_lo = slot;
+    p->fw_n = 1;
+    const unsigned grid = std::min<unsigned>(kore_div_up(p->np, 256), 64u);
+    std::vector<double> red(grid);
+    double *d_red = p->d_part;
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 1, true));
+    int s;
+    if (p->prec == KORE_PREC_FP64) {
+        k_rowinfo<double2><<<dim3(grid, 1), 256, 0, p->stream>>>(make_fv<double2>(p), d_red);
+        if (p->ell_stride() > 0)
+            k_ell_fill<double2><<<dim3(std::min<unsigned>(kore_div_up(p->ell_stride(), 256), 4096u), 1), 256, 0,
+                              p->stream>>>(p->ell_stride(), p->ell_w, (p->S + 31) / 32, p->S, p->np, p->d_ell_src,
+                                           p->d_aval, p->d_rscale + (int64_t)slot * p->np,
+                                           static_cast<double2 *>(p->d_ell_val) + (int64_t)slot * p->ell_stride());
+        KORE_LAUNCHED(2);
+        s = factor_dispatch<double2>(p);
+    } else {
+        k_rowinfo<float2><<<dim3(grid, 1), 256, 0, p->stream>>>(make_fv<float2>(p), d_red);
+        if (p->ell_stride() > 0)
+            k_ell_fill<float2><<<dim3(std::min<unsigned>(kore_div_up(p->ell_stride(), 256), 4096u), 1), 256, 0,
+                              p->stream>>>(p->ell_stride(), p->ell_w, (p->S + 31) / 32, p->S, p->np, p->d_ell_src,
+                                           p->d_aval, p->d_rscale + (int64_t)slot * p->np,
+                                           static_cast<float2 *>(p->d_ell_val) + (int64_t)slot * p->ell_stride());
+        KORE_LAUNCHED(2);
+        s = factor_dispatch<float2>(p);
+    }
+    p->fw_lo = 0;
+    p->fw_n = p->nshift;
+    if (s != KORE_OK) return s;
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 1, false));
+    KORE_CUDA_TRY(cudaMemcpyAsync(red.data(), d_red, red.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+    KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    double mx = 0.0;
+    for (unsigned b = 0; b < grid; ++b) mx = std::max(mx, red[b]);
+    p->minfs[slot] = mx;
+    if (slot == 0) p->minf = mx;
+    KORE_CUDA_TRY(cudaMemcpyAsync(p->d_minf + slot, &p->minfs[slot], sizeof(double), cudaMemcpyHostToDevice,
                                   p->stream));
     KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
     KORE_TRY(kore_check_device_error(p));

@@ -4,7 +4,7 @@
 //     a b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi      (FP32 accumulation in tensor memory)
 // and each complex product as four real ones,
 //     Re(AB) = Ar Br - Ai Bi,  Im(AB) = Ar Bi + Ai Br,
-// the subtraction done by the MMA's negate-A bit.
+// the subtraction done by the -Im planes of the B operand (below), so every MMA adds.
 //
 // Data flow of one 128 x 64 tile of C = beta C + alpha (A1 B1 [+ A2 B2]):
 //   * k_tc_split writes, once per matrix, K-major FP32 planes: Re hi, Re lo, Im hi, Im lo
@@ -396,22 +396,23 @@ void kore_tc_level_bytes(const kore_plan *p, int cap, int64_t *plane_bytes, int6
 // tensor-core form of k_even_gemm: D_i -= L_q H_jl + U_q G_jr;  L' = -L_q G_jl;
 // U' = -U_q H_jr.
 int kore_even_update_tc(kore_plan *p, const BcrLevel &lv) {
-    const int S = p->S, ns = p->nshift;
+    const int S = p->S, ns = p->fw_n;
+    const int64_t lo = p->fw_lo;   // shift sh of the factor window is shift lo + sh of the plan
     const int64_t SS = (int64_t)S * S;
     std::vector<const float2 *> src;   // A operands, then B operands
     std::vector<TcJob> jobs;
     const int64_t nA = 2 * (int64_t)lv.neven * ns, nB = 2 * (int64_t)lv.nodd * ns;
     src.reserve(nA + nB);
     for (int sh = 0; sh < ns; ++sh) {
-        const float2 *LU = static_cast<const float2 *>(p->d_LU) + sh * p->lu_stride();
+        const float2 *LU = static_cast<const float2 *>(p->d_LU) + (lo + sh) * p->lu_stride();
         for (int e = 0; e < lv.neven; ++e) {
             src.push_back(LU + (lv.lu_L + 2 * e) * SS);   // A index (sh neven + e) 2 + 0: L_q
             src.push_back(LU + (lv.lu_U + 2 * e) * SS);   //                            + 1: U_q
         }
     }
     for (int sh = 0; sh < ns; ++sh) {
-        const float2 *G = static_cast<const float2 *>(p->d_Gm) + sh * p->f_stride();
-        const float2 *H = static_cast<const float2 *>(p->d_Hm) + sh * p->f_stride();
+        const float2 *G = static_cast<const float2 *>(p->d_Gm) + (lo + sh) * p->f_stride();
+        const float2 *H = static_cast<const float2 *>(p->d_Hm) + (lo + sh) * p->f_stride();
         for (int o = 0; o < lv.nodd; ++o) {
             const int64_t j = (int64_t)(2 * o + 1) * lv.stride;
             src.push_back(G + j * SS);                    // B index (sh nodd + o) 2 + 0: G_j
@@ -419,8 +420,8 @@ int kore_even_update_tc(kore_plan *p, const BcrLevel &lv) {
         }
     }
     for (int sh = 0; sh < ns; ++sh) {
-        float2 *LU = static_cast<float2 *>(p->d_LU) + sh * p->lu_stride();
-        float2 *Dw = static_cast<float2 *>(p->d_Dw) + sh * p->f_stride();
+        float2 *LU = static_cast<float2 *>(p->d_LU) + (lo + sh) * p->lu_stride();
+        float2 *Dw = static_cast<float2 *>(p->d_Dw) + (lo + sh) * p->f_stride();
         for (int e = 0; e < lv.neven; ++e) {
             const int q = 2 * e;
             const bool hasl = q >= 1, hasr = q + 1 < lv.Kl;
@@ -487,16 +488,19 @@ int tc_upload_run(kore_plan *p, const std::vector<const float2 *> &src, int64_t 
 // G0 and H0 come from the sparse couplings (k_gh_l0); R goes to the Gauss-Jordan work
 // area T, free after the extraction.
 int kore_gh_update_tc(kore_plan *p, const BcrLevel &lv, int level0) {
-    const int S = p->S, ns = p->nshift;
+    const int S = p->S, ns = p->fw_n;
+    const int64_t lo = p->fw_lo;   // shift sh of the factor window is shift lo + sh of the plan
     const int64_t SS = (int64_t)S * S, no = lv.nodd;
     float2 *Dinv = static_cast<float2 *>(p->d_Dinv), *Dw = static_cast<float2 *>(p->d_Dw);
     float2 *G = static_cast<float2 *>(p->d_Gm), *H = static_cast<float2 *>(p->d_Hm);
     float2 *LU = static_cast<float2 *>(p->d_LU), *T = static_cast<float2 *>(p->d_T);
-    auto blk = [&](float2 *base, int sh, int64_t o) { return base + sh * p->f_stride() + (2 * o + 1) * lv.stride * SS; };
+    auto blk = [&](float2 *base, int sh, int64_t o) {
+        return base + (lo + sh) * p->f_stride() + (2 * o + 1) * lv.stride * SS;
+    };
     // residual storage of (shift, odd o, side)
     auto rstore = [&](int sh, int64_t o, int side) -> float2 * {
-        if (level0) return T + sh * p->t_stride() + o * 2 * SS + side * SS;
-        return LU + sh * p->lu_stride() + ((side ? lv.lu_U : lv.lu_L) + 2 * o + 1) * SS;
+        if (level0) return T + (lo + sh) * p->t_stride() + o * 2 * SS + side * SS;
+        return LU + (lo + sh) * p->lu_stride() + ((side ? lv.lu_U : lv.lu_L) + 2 * o + 1) * SS;
     };
     auto hasr = [&](int64_t o) { return 2 * o + 2 < lv.Kl; };
     std::vector<const float2 *> src;
@@ -532,7 +536,8 @@ int kore_gh_update_tc(kore_plan *p, const BcrLevel &lv, int level0) {
     KORE_TRY(tc_upload_run(p, src, ns * no, jobs));
     if (level0) {
         k_add_couplings<<<dim3((unsigned)no, 2, ns), 256, 0, p->stream>>>(p->d_cc_ptr, p->d_cc_row, p->d_cc_src,
-                                                                          p->d_aval, p->d_rscale, S, p->np, T,
+                                                                          p->d_aval, p->d_rscale + lo * p->np, S,
+                                                                          p->np, T + lo * p->t_stride(),
                                                                           p->t_stride());
         KORE_LAUNCHED(1);
     }

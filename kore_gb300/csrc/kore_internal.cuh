@@ -75,6 +75,9 @@ struct kore_plan {
     bool factored = false;
     // factorised shifts: every factor buffer holds shift_cap sets, shift s at offset s * stride
     int nshift = 0, shift_cap = 0;
+    // factor window: the shifts [fw_lo, fw_lo + fw_n) that the factorisation kernels work
+    // on (all of them for kore_factor_shifts, one for a slot refill)
+    int fw_lo = 0, fw_n = 0;
     std::vector<double2> sigmas;      // host copy of the shifts
     std::vector<double> minfs;        // ||A - sigma_s B||_inf per shift
     double2 *d_sigma = nullptr;       // device copy of the shifts
@@ -140,11 +143,13 @@ struct kore_plan {
     int *d_cnt = nullptr;             // sweep completion counters (shift_cap x sweep_stages() x K)
     IrState *d_ir = nullptr;          // one per shift
 
-    // Krylov-Schur workspace
-    double2 *d_V = nullptr;           // np x (ncv+1)
-    double2 *d_Vtmp = nullptr;        // np x (ncv+1)
-    int ks_cap = 0;
-    double2 *d_small = nullptr;
+    // Krylov-Schur workspace (per target: basis and restart buffer of ncv + 1 columns)
+    double2 *d_V = nullptr;           // np x ks_cap
+    double2 *d_Vtmp = nullptr;        // np x ks_cap
+    double2 *d_ksx = nullptr;         // np x targets: gathered input vectors of the sparse products
+    int64_t ks_cap = 0;               // columns of d_V, d_Vtmp
+    double2 *d_small = nullptr;       // projected problems, Gram-Schmidt coefficients and partial sums
+    int ks_small_cap = 0;             // targets d_small holds
 
     size_t bytes = 0;
     size_t factor_bytes = 0;          // bytes of the per-shift buffers
@@ -175,6 +180,9 @@ int kore_alloc(kore_plan *p, void **ptr, size_t bytes);
 void kore_build_levels(kore_plan *p);
 // factorise A - sigma_s B for nshift shifts (interleaved re, im) at once
 int kore_factor_impl(kore_plan *p, int nshift, const double *sigmas, int precision);
+// re-factorise shift `slot` of a factorised plan for a new shift, in the plan's
+// precision; the other shifts' factors are kept
+int kore_factor_slot(kore_plan *p, int slot, double sigma_re, double sigma_im);
 
 // gemm_tc.cu: tensor-core (tcgen05, 3xTF32) even-block update of a level >= 1, complex64
 int kore_even_update_tc(kore_plan *p, const BcrLevel &lv);
@@ -187,11 +195,20 @@ void kore_tc_level_bytes(const kore_plan *p, int cap, int64_t *plane_bytes, int6
 // x_s = (A - sigma_s B)^-1 b_s for every factorised shift s on padded l-major
 // complex128 vectors (device; shift s at offset s * np), refined in FP64 when the
 // factors are complex64 (asynchronous; counters in the plan's per-shift IrState).
-int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol);
+// live_mask: only the shifts s < 32 whose bit is set are solved (the others' x is left
+// as it is); shifts past 31 are always solved.
+// shift_tols (host, nshift entries, may be null): per-shift refinement tolerances in
+// place of tol (entries <= 0 use tol).
+int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol, unsigned live_mask = ~0u,
+                       const double *shift_tols = nullptr);
 int kore_ir_reset(kore_plan *p);
 int kore_ir_read(kore_plan *p, IrState *out);
 // y = B x on padded vectors
 int kore_spmv_b(kore_plan *p, const double2 *x, double2 *y);
+// y_s = B x_s for the factorised shifts s in live_mask (vectors at offset s * np)
+int kore_spmv_b_shifts(kore_plan *p, const double2 *x, double2 *y, unsigned live_mask);
+// y_s = A x_s for the factorised shifts s in live_mask
+int kore_spmv_a_shifts(kore_plan *p, const double2 *x, double2 *y, unsigned live_mask);
 // y = A x - lam B x on padded vectors
 int kore_spmv_pencil(kore_plan *p, double lre, double lim, const double2 *x, double2 *y);
 int kore_gather(kore_plan *p, const double2 *orig, double2 *padded);
@@ -201,5 +218,6 @@ int kore_gather_shifts(kore_plan *p, const double2 *orig, double2 *padded);
 int kore_scatter_shifts(kore_plan *p, const double2 *padded, double2 *orig);
 
 // eigs.cu
-int kore_eigs_impl(kore_plan *p, const kore_eps_opts *o, double *evals, double *evecs,
+// ntarget Krylov-Schur runs, target t around factorised shift t (ntarget = nshift)
+int kore_eigs_impl(kore_plan *p, int ntarget, const kore_eps_opts *o, double *evals, double *evecs,
                    int max_pairs, int *nconv, kore_stats *st);

@@ -95,7 +95,7 @@ void free_plan(kore_plan *p) {
     void *ptrs[] = {p->d_arow, p->d_acol, p->d_asplit, p->d_aval, p->d_brow, p->d_bcol, p->d_bval,
                     p->d_slot2orig, p->d_bsz, p->d_Dinv, p->d_Gm, p->d_Hm, p->d_Dw, p->d_LU, p->d_lev,
                     p->d_rscale, p->d_T, p->d_piv, p->d_pidx, p->d_used, p->d_zlo, p->d_xlo, p->d_flo,
-                    p->d_red, p->d_part, p->d_err, p->d_bar, p->d_ir, p->d_V, p->d_Vtmp, p->d_small,
+                    p->d_red, p->d_part, p->d_err, p->d_bar, p->d_ir, p->d_V, p->d_Vtmp, p->d_ksx, p->d_small,
                     p->d_sigma, p->d_minf, p->d_bb, p->d_xb, p->d_rb, p->d_bn, p->d_rn, p->d_cnt,
                     p->d_ell_col, p->d_ell_src, p->d_ell_val, p->d_long_rows, p->d_srow, p->d_smid,
                     p->d_scol, p->d_sval, p->d_cc_ptr, p->d_cc_row, p->d_cc_src};
@@ -464,7 +464,16 @@ int kore_eigs(kore_plan *p, const kore_eps_opts *opts, double *evals, double *ev
     if (p->factored && p->nshift != 1) return KORE_EINVAL;
     DeviceGuard g(p->device);
     *nconv = 0;
-    return kore_eigs_impl(p, opts, evals, evecs, max_pairs, nconv, stats);
+    return kore_eigs_impl(p, 1, opts, evals, evecs, max_pairs, nconv, stats);
+}
+
+int kore_eigs_shifts(kore_plan *p, int ntarget, const kore_eps_opts *opts, double *evals, double *evecs,
+                     int max_pairs, int *nconv, kore_stats *stats) {
+    if (!p || ntarget <= 0 || !opts || !evals || !nconv || max_pairs <= 0) return KORE_EINVAL;
+    if (p->factored && ntarget < p->nshift) return KORE_EINVAL;
+    DeviceGuard g(p->device);
+    for (int t = 0; t < ntarget; ++t) nconv[t] = 0;
+    return kore_eigs_impl(p, ntarget, opts, evals, evecs, max_pairs, nconv, stats);
 }
 
 int kore_residual(kore_plan *p, double lre, double lim, const double *x, double *y) {
@@ -590,8 +599,9 @@ int kore_plan_estimate_bytes(const kore_pencil_desc *d, int precision, int nshif
     }
     b += c * (3 * np * 16 + 2 * (np / 64 + np / 8 + 1024) * 8 + (nlev > 0 ? 3 * nlev + 2 : 1) * K * 4 + ell * e + 128);
     b += 2 * d->n * c * 16;   // kore_solve's device copies of b and x
-    // Krylov basis, its copy and the projected-problem workspace
-    if (ncv > 0) b += 2 * np * (int64_t)(ncv + 1) * 16 + (int64_t)(65 * 64 * 4 + 8 * 65 + 2048 * 65 + 4096) * 16;
+    // per target (one per shift): Krylov basis, its restart copy, a gathered input vector
+    // and the projected-problem workspace
+    if (ncv > 0) b += c * (2 * np * (int64_t)(ncv + 1) * 16 + np * 16 + (int64_t)(65 * 64 * 4 + 8 * 65 + 2048 * 65 + 4096) * 16);
     b += 128LL << 20;   // allocation granularity of ~50 buffers
     *bytes = b;
     return KORE_OK;

@@ -53,11 +53,17 @@ struct SweepArgs {
     int *err;
     const int *skip;                 // shift s is skipped when skip[s * skip_stride] != 0
     int skip_stride;
+    unsigned live_mask;              // shift s (< 32) takes part only when bit s is set
     int *count;                      // sweeps that ran
     int *count_total;
 };
 
 constexpr int kMaxLevels = 24;
+
+// bit s of a live-shift mask (shifts past 31 always take part)
+__host__ __device__ __forceinline__ bool mask_has(unsigned mask, int64_t s) {
+    return s >= 32 || ((mask >> s) & 1u);
+}
 
 __device__ __forceinline__ void st_release_cta(long long *p, long long v) {
     asm volatile("st.release.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(p)), "l"(v) : "memory");
@@ -218,9 +224,10 @@ __global__ void __launch_bounds__(kTmaThreads, kTmaCtasPerSm) k_sweep_tma(const 
     __shared__ BcrLevel lv_s[kMaxLevels];
     __shared__ int64_t st_begin[3 * kMaxLevels + 2];
     __shared__ long long ready;      // highest tile of this CTA whose inputs are complete
-    if (a.skip) {
+    {
         bool all = true;
-        for (int s = 0; s < ns; ++s) all = all && (a.skip[s * a.skip_stride] != 0);
+        for (int s = 0; s < ns; ++s)
+            all = all && (!mask_has(a.live_mask, s) || (a.skip && a.skip[s * a.skip_stride] != 0));
         if (all) return;
     }
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -251,7 +258,9 @@ __global__ void __launch_bounds__(kTmaThreads, kTmaCtasPerSm) k_sweep_tma(const 
     }
     __syncthreads();
     const int64_t total = st_begin[nstage];
-    auto live = [&](int64_t s) -> bool { return !(a.skip && a.skip[s * a.skip_stride] != 0); };
+    auto live = [&](int64_t s) -> bool {
+        return mask_has(a.live_mask, s) && !(a.skip && a.skip[s * a.skip_stride] != 0);
+    };
     auto ctr = [&](int64_t s, int sid, int64_t blk) -> int * { return a.cnt + ((s * nstage + sid) * K + blk); };
     auto xready = [&](int64_t s, int64_t blk) -> int * {
         if (blk == 0) return ctr(s, 2 * L, 0);
@@ -550,6 +559,7 @@ struct SpmvArgs {
     double *part;           // mode 2: per-CTA maxima of |y| and |x|, part[s * 2 gridDim.x + 2 blockIdx.x (+1)]
     const int *skip;        // shift s is skipped when skip[s * skip_stride] != 0
     int skip_stride;
+    unsigned live_mask;     // shift s (< 32) is computed only when bit s is set
 };
 
 // acc += sum over the values sub, sub + LANES, ... of [e0, e1) of val[e] x[col[e]]
@@ -602,7 +612,7 @@ __device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long v
 
 __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
     const int64_t s = blockIdx.y;
-    if (a.skip && a.skip[s * a.skip_stride]) return;
+    if (!mask_has(a.live_mask, s) || (a.skip && a.skip[s * a.skip_stride])) return;
     const int64_t np = a.np;
     const double2 *x = a.x + s * np;
     double2 *y = a.y + s * np;
@@ -695,6 +705,7 @@ SweepArgs sweep_args(const kore_plan *p, int nshift) {
     a.f_stride = p->f_stride(); a.lu_stride = p->lu_stride();
     a.ell_col = p->d_ell_col; a.ell_val = p->d_ell_val; a.ell_w = p->ell_w; a.ell_stride = p->ell_stride();
     a.rscale = p->d_rscale;
+    a.live_mask = ~0u;
     return a;
 }
 
@@ -740,9 +751,11 @@ int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st) {
     return KORE_OK;
 }
 
-int sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int accumulate, const int *skip) {
+int sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int accumulate, const int *skip,
+          unsigned live_mask) {
     if (p->prof) KORE_TRY(kore_prof_mark(p, 0, true));
     SweepArgs a = sweep_args(p, p->nshift);
+    a.live_mask = live_mask;
     a.b = b; a.bnorm = bnorm;
     a.f = p->d_flo; a.z = p->d_zlo; a.x = p->d_xlo;
     a.out = x; a.accumulate = accumulate; a.cnt = p->d_cnt; a.err = p->d_err;
@@ -779,6 +792,7 @@ SpmvArgs spmv_args(const kore_plan *p, int mode, const double2 *x, double2 *y) {
     a.lam = mk(0.0, 0.0); a.sig = nullptr;
     a.x = x; a.rhs = nullptr; a.y = y; a.part = nullptr;
     a.skip = nullptr; a.skip_stride = 0;
+    a.live_mask = ~0u;
     return a;
 }
 
@@ -788,6 +802,30 @@ int kore_spmv_b(kore_plan *p, const double2 *x, double2 *y) {
     if (!p->has_b) return KORE_EINVAL;
     if (p->prof) KORE_TRY(kore_prof_mark(p, 2, true));
     k_spmv<<<spmv_grid(p), 256, 0, p->stream>>>(spmv_args(p, 0, x, y));
+    KORE_LAUNCHED(1);
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 2, false));
+    KORE_CUDA_TRY(cudaGetLastError());
+    return KORE_OK;
+}
+
+int kore_spmv_b_shifts(kore_plan *p, const double2 *x, double2 *y, unsigned live_mask) {
+    if (!p->has_b) return KORE_EINVAL;
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 2, true));
+    SpmvArgs a = spmv_args(p, 0, x, y);
+    a.live_mask = live_mask;
+    k_spmv<<<dim3(spmv_grid(p), std::max(1, p->nshift)), 256, 0, p->stream>>>(a);
+    KORE_LAUNCHED(1);
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 2, false));
+    KORE_CUDA_TRY(cudaGetLastError());
+    return KORE_OK;
+}
+
+int kore_spmv_a_shifts(kore_plan *p, const double2 *x, double2 *y, unsigned live_mask) {
+    if (p->prof) KORE_TRY(kore_prof_mark(p, 2, true));
+    SpmvArgs a = spmv_args(p, 1, x, y);   // A x - 0 B x
+    a.has_b = 0;
+    a.live_mask = live_mask;
+    k_spmv<<<dim3(spmv_grid(p), std::max(1, p->nshift)), 256, 0, p->stream>>>(a);
     KORE_LAUNCHED(1);
     if (p->prof) KORE_TRY(kore_prof_mark(p, 2, false));
     KORE_CUDA_TRY(cudaGetLastError());
@@ -838,9 +876,13 @@ int kore_scatter_shifts(kore_plan *p, const double2 *padded, double2 *orig) {
 namespace {
 
 // one thread per shift
-__global__ void k_ir_begin(IrState *st, int nshift) {
+__global__ void k_ir_begin(IrState *st, int nshift, unsigned live_mask) {
     const int s = threadIdx.x;
     if (s >= nshift) return;
+    if (!mask_has(live_mask, s)) {   // not part of this application: nothing to refine
+        st[s].done = 1;
+        return;
+    }
     st[s].done = 0;
     st[s].prev = 1e300;
     st[s].applies += 1;
@@ -849,9 +891,16 @@ __global__ void k_ir_begin(IrState *st, int nshift) {
 // One CTA per shift s: eta = ||r||_inf / (||M||_inf ||x||_inf + ||b||_inf) from the
 // per-CTA maxima of the residual kernel; stop when eta <= tol or when it no longer
 // decreases (FP64 floor).
+// Per-shift refinement tolerances of one application (shifts past 31 use the scalar).
+struct ShiftTols {
+    double t[32];
+    int valid;
+};
+
 __global__ void k_ir_check(const double *__restrict__ part, int n, const double *__restrict__ bnorm,
-                           const double *__restrict__ minf, double tol, IrState *stall, double *rn) {
+                           const double *__restrict__ minf, double tol0, ShiftTols tols, IrState *stall, double *rn) {
     const int s = blockIdx.x;
+    const double tol = (tols.valid && s < 32) ? tols.t[s] : tol0;
     IrState *st = stall + s;
     if (st->done) return;
     part += (int64_t)s * 2 * n;
@@ -870,7 +919,8 @@ __global__ void k_ir_check(const double *__restrict__ part, int n, const double 
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { rb = max(rb, s0[w]); xb = max(xb, s1[w]); }
     const double rm = __longlong_as_double((long long)rb), xm = __longlong_as_double((long long)xb);
     const double den = minf[s] * xm + bnorm[s];
-    const double eta = (den > 0.0) ? rm / den : 0.0;
+    // a NaN in r, x or b makes eta NaN (a NaN denominator must not read as converged)
+    const double eta = (den == 0.0) ? 0.0 : rm / den;
     if (!(eta == eta)) {
         st->nan = 1;
         st->done = 1;
@@ -902,27 +952,32 @@ __global__ void k_ir_end(IrState *st, int nshift) {
 // the remaining work of that shift is skipped (kernels return at once when every
 // shift is done).
 constexpr int kIrMax = 6;
-int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol) {
+int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol, unsigned live_mask,
+                       const double *shift_tols) {
     if (!p->factored) return KORE_ENOTFACTORED;
     double *bn = p->d_bn, *rn = p->d_rn;
     KORE_TRY(absmax(p, b, bn, p->d_part));
-    if (p->prec != KORE_PREC_MIXED) return sweep(p, b, bn, x, 0, nullptr);
+    if (p->prec != KORE_PREC_MIXED) return sweep(p, b, bn, x, 0, nullptr, live_mask);
     if (!(tol > 0.0)) tol = 1e-14;
+    ShiftTols tols{};
+    tols.valid = shift_tols ? 1 : 0;
+    for (int s = 0; s < 32 && shift_tols && s < p->nshift; ++s) tols.t[s] = (shift_tols[s] > 0.0) ? shift_tols[s] : tol;
     const int ns = p->nshift;
     const int skip_stride = (int)(sizeof(IrState) / sizeof(int));
-    k_ir_begin<<<1, ns, 0, p->stream>>>(p->d_ir, ns);
+    k_ir_begin<<<1, ns, 0, p->stream>>>(p->d_ir, ns, live_mask);
     KORE_LAUNCHED(1);
-    KORE_TRY(sweep(p, b, bn, x, 0, nullptr));
+    KORE_TRY(sweep(p, b, bn, x, 0, nullptr, live_mask));
     const unsigned grid = spmv_grid(p);
     SpmvArgs ra = spmv_args(p, 2, x, p->d_rb);
     ra.sig = p->d_sigma; ra.rhs = b; ra.part = p->d_part; ra.skip = &p->d_ir->done; ra.skip_stride = skip_stride;
+    ra.live_mask = live_mask;
     for (int it = 0; it < kIrMax; ++it) {
         if (p->prof) KORE_TRY(kore_prof_mark(p, 2, true));
         k_spmv<<<dim3(grid, ns), 256, 0, p->stream>>>(ra);
-        k_ir_check<<<ns, 1024, 0, p->stream>>>(p->d_part, (int)grid, bn, p->d_minf, tol, p->d_ir, rn);
+        k_ir_check<<<ns, 1024, 0, p->stream>>>(p->d_part, (int)grid, bn, p->d_minf, tol, tols, p->d_ir, rn);
         KORE_LAUNCHED(2);
         if (p->prof) KORE_TRY(kore_prof_mark(p, 2, false));
-        KORE_TRY(sweep(p, p->d_rb, rn, x, 1, &p->d_ir->done));
+        KORE_TRY(sweep(p, p->d_rb, rn, x, 1, &p->d_ir->done, live_mask));
     }
     k_ir_end<<<1, ns, 0, p->stream>>>(p->d_ir, ns);
     KORE_LAUNCHED(1);
@@ -963,8 +1018,9 @@ int kore_ir_read(kore_plan *p, IrState *out) {
 // latency-critical loop, or a host library that is handed only a stream.  For them the
 // scratch of one solve (padded right-hand side and solution, the reduction vectors of
 // the sweep, the FP64 residual and the per-CTA maxima of the refinement loop, the
-// grid-barrier counter, the error flag and the refinement state) lives in the
-// file-scope array below instead of in buffers of the plan or of a caller.  Its size
+// norm partials, the refinement state, the sweep's completion counters and the error
+// flag) lives in the file-scope array below instead of in buffers of the plan or of a
+// caller.  Its size
 // is fixed at kNoAllocMaxNp padded unknowns (about 1.6 MB, held by every GPU that
 // loads the library until the process exits); larger problems are rejected.
 // The kernels are the ones of kore_solve_dev; only their scratch pointers differ.
@@ -1039,7 +1095,7 @@ int noalloc_solve(kore_plan *p, NoAllocScratch *s, const double2 *b_dev, double2
         KORE_TRY(noalloc_sweep<double2>(p, s, s->bp, bn, s->xp, 0, nullptr, st));
     } else {
         if (!(tol > 0.0)) tol = 1e-14;
-        k_ir_begin<<<1, 1, 0, st>>>(&s->ir, 1);
+        k_ir_begin<<<1, 1, 0, st>>>(&s->ir, 1, ~0u);
         KORE_LAUNCHED(1);
         KORE_TRY(noalloc_sweep<float2>(p, s, s->bp, bn, s->xp, 0, nullptr, st));
         const unsigned grid = spmv_grid(p);
@@ -1047,7 +1103,7 @@ int noalloc_solve(kore_plan *p, NoAllocScratch *s, const double2 *b_dev, double2
         ra.lam = mk(p->sigma_re, p->sigma_im); ra.rhs = s->bp; ra.part = s->part; ra.skip = &s->ir.done;
         for (int it = 0; it < kIrMax; ++it) {
             k_spmv<<<grid, 256, 0, st>>>(ra);
-            k_ir_check<<<1, 1024, 0, st>>>(s->part, (int)grid, bn, p->d_minf, tol, &s->ir, rn);
+            k_ir_check<<<1, 1024, 0, st>>>(s->part, (int)grid, bn, p->d_minf, tol, ShiftTols{}, &s->ir, rn);
             KORE_LAUNCHED(2);
             KORE_TRY(noalloc_sweep<float2>(p, s, s->r, rn, s->xp, 1, &s->ir.done, st));
         }
@@ -1071,6 +1127,11 @@ extern "C" int kore_solve_dev_noalloc(kore_plan *p, const void *b_dev, void *x_d
         return KORE_EINVAL;
     }
     if (!p->factored) return KORE_ENOTFACTORED;
+    if (p->nshift != 1) {
+        std::fprintf(stderr, "kore_solve_dev_noalloc: the plan holds %d factorised shifts; this entry point "
+                             "solves with a plan of one shift (kore_factor)\n", p->nshift);
+        return KORE_EINVAL;
+    }
     int prev = -1;
     cudaGetDevice(&prev);
     if (prev != p->device) KORE_CUDA_TRY(cudaSetDevice(p->device));

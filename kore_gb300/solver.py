@@ -95,7 +95,7 @@ class Pencil:
 
     # -- factor / solve ---------------------------------------------------------------
     def factor(self, sigma, precision="fp64"):
-        """Factorise A - sigma*B (block Thomas, see csrc/factor.cu)."""
+        """Factorise A - sigma*B (block cyclic reduction, csrc/factor.cu)."""
         sigma = complex(sigma)
         t = time.perf_counter()
         L.check(self.lib.kore_factor(self._plan, sigma.real, sigma.imag, L.PREC[precision]), "kore_factor")
@@ -210,6 +210,51 @@ def forced_sweep(pencil, omegas, b, precision="mixed", group=16, refine_tol=0.0,
     return X, times
 
 
+def eigs_targets(pencil, targets, nev, which="TM", precision="mixed", tol=1e-15, maxit=50, seeds=None, ncv=0,
+                 purify=True, refine_tol=0.0, vectors=True, slots=None):
+    """Shift-and-invert Krylov-Schur at several targets of one pencil, the targets
+    stepping together in shared launches (``kore_eigs_shifts``).  ``slots`` targets run
+    at a time (default: all); when one finishes, the next takes its slot (its shift is
+    factorised then), so a long list of targets keeps every slot busy.
+
+    The reference computes one target per ``bin/solve.py`` run (``bin/solve.py:91-158``,
+    with ``tau`` from ``parameters.py``), fanned out over parameter sweeps by its tools;
+    target t here gives what that run gives: the converged eigenvalues nearest ``tau_t``
+    in SLEPc's order for ``which`` and their unit eigenvectors.  ``nev`` and ``seeds``
+    may be one value or one per target.  Factorises ``A - tau_t B`` for every target
+    first (one batched factorisation).
+
+    Returns a list of (eigenvalues, eigenvectors or None, stats dict), one per target.
+    """
+    tg = np.asarray(targets, dtype=np.complex128).ravel()
+    T = len(tg)
+    nevs = np.broadcast_to(np.asarray(nev, dtype=int), (T,))
+    sds = np.broadcast_to(np.asarray(seeds if seeds is not None else np.arange(T), dtype=np.uint64), (T,))
+    ns = T if slots is None else max(1, min(int(slots), T))
+    pencil.factor_shifts(tg[:ns], precision)
+    opts = (L.EpsOpts * T)()
+    mx = 0
+    for t in range(T):
+        k = int(nevs[t])
+        m = int(ncv) or min(pencil.n, max(2 * k, k + 15))
+        mx = max(mx, m)
+        opts[t] = L.EpsOpts(nev=k, ncv=int(ncv), tol=tol, maxit=maxit, which=L.WHICH[which], target_re=tg[t].real,
+                            target_im=tg[t].imag, seed=int(sds[t]), purify=int(purify),
+                            refine_tol=refine_tol)
+    ev = np.zeros((T, mx), dtype=np.complex128)
+    X = np.zeros((T, mx, pencil.n), dtype=np.complex128) if vectors else None
+    nconv = (C.c_int * T)()
+    st = (L.Stats * T)()
+    s = pencil.lib.kore_eigs_shifts(pencil._plan, T, opts, L.ptr(ev), L.ptr(X) if vectors else None, mx, nconv, st)
+    if s not in (L.KORE_OK, 5):   # KORE_ENOCONV: a target with nconv = 0
+        L.check(s, "kore_eigs_shifts")
+    out = []
+    for t in range(T):
+        k = nconv[t]
+        out.append((ev[t, :k].copy(), np.ascontiguousarray(X[t, :k].T) if vectors else None, st[t].as_dict()))
+    return out
+
+
 class EPS:
     """Shift-and-invert Krylov-Schur eigensolver with the slepc4py EPS call sequence
     that ``bin/solve.py:91-123`` uses."""
@@ -238,6 +283,7 @@ class EPS:
         self.precision = "fp64"
         self.seed = 0
         self.purify = True
+        self.purify_steps = 1
         self.refine_tol = 0.0
         self._lam = np.zeros(0, complex)
         self._X = None
@@ -292,6 +338,8 @@ class EPS:
             self.maxit = int(o["eps_max_it"])
         if "eps_purify" in o:
             self.purify = str(o["eps_purify"]).lower() not in ("0", "false", "no")
+        if "kore_purify_steps" in o:
+            self.purify_steps = int(o["kore_purify_steps"])
         if "kore_precision" in o:
             self.precision = o["kore_precision"]
         if "kore_seed" in o:
@@ -320,7 +368,7 @@ class EPS:
         nev, ncv, _ = self.getDimensions()
         o = L.EpsOpts(nev=nev, ncv=ncv, tol=self.tol, maxit=self.maxit, which=L.WHICH[self.which],
                       target_re=self.target.real, target_im=self.target.imag, seed=self.seed,
-                      purify=1 if self.purify else 0, refine_tol=self.refine_tol)
+                      purify=self.purify_steps if self.purify else 0, refine_tol=self.refine_tol)
         ev = np.zeros(ncv, dtype=np.complex128)
         X = np.zeros((ncv, p.n), dtype=np.complex128)
         nconv = C.c_int(0)

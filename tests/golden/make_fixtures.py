@@ -12,11 +12,11 @@ For each case this script
   4. stores A, B (or the forcing column) and the derived sizes in
      ``tests/golden/<case>.npz``.
 
-It needs the reference checkout (default ``/root/reference``, or ``$KORE_REF``) and
-is run by hand; the fixtures it writes are committed so that the tests never read
-the reference at run time.
+It needs a checkout of the reference, named by ``$KORE_REF``, and is run by hand;
+the fixtures it writes are committed so that the tests never read the reference at
+run time.
 
-    python tests/golden/make_fixtures.py [case ...]
+    KORE_REF=<kore checkout> python tests/golden/make_fixtures.py [case ...]
 """
 import json
 import os
@@ -29,7 +29,7 @@ import tempfile
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("KORE_REF", "/root/reference")
+REF = os.environ.get("KORE_REF", "")
 STANDIN = os.path.join(HERE, "_standin")
 
 # case name -> (base parameter file relative to the reference root, overrides, needs profiles)
@@ -174,6 +174,8 @@ def make_any(name):
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(os.path.join(REF, "bin")):
+        sys.exit("set KORE_REF to a checkout of the reference (the directory holding bin/assemble.py)")
     names = sys.argv[1:] or list(CASES) + list(RA_PAIRS)
     from concurrent.futures import ProcessPoolExecutor
     with ProcessPoolExecutor(max_workers=min(4, len(names))) as ex:
