@@ -91,13 +91,14 @@ typedef struct {
     int32_t ncv;          /* 0 = SLEPc default */
     double  tol;          /* relative, on the transformed eigenvalue theta */
     int32_t maxit;        /* restarts */
-    int32_t which;        /* KORE_WHICH_* */
+    int32_t which;        /* KORE_WHICH_TM, _TR or _TI: shift-and-invert needs a target
+                             criterion (SLEPc refuses the others under sinvert) */
     double  target_re, target_im;   /* tau; must equal the factorised shift */
     uint64_t seed;        /* start vector: complex standard normal from this seed */
     int32_t purify;       /* applications of OP to each eigenvector before it is
                              returned: 1 is SLEPc's default purification, 0 none */
     double  refine_tol;   /* mixed precision: relative residual of each OP application
-                             (<= 0 selects 1e-15); the purifying application of the
+                             (<= 0 selects 1e-16); the purifying application of the
                              eigenvectors is refined until the residual stops decreasing */
 } kore_eps_opts;
 
@@ -293,6 +294,16 @@ int kore_batch_destroy(kore_batch *batch);
  * No counterpart in the reference; a diagnostic for the kernel.
  */
 int kore_tc_selftest(int device, int S, int nmat, double *max_rel_err);
+
+/*
+ * Multiplication operator of the Gegenbauer (ultraspherical) basis, computed on
+ * `device`: M multiplies a C^(lam) series by the function whose N C^(lam) coefficients
+ * are a0 (lam >= 0; lam = 0 is the Chebyshev basis).  M is banded with half-width
+ * h >= (index of the last nonzero of a0) + 1; band receives N (2h + 1) doubles,
+ * band[(d + h) N + j] = M[j, j + d] for |d| <= h (0 outside the matrix).  Replaces Mlam
+ * (bin/utils.py:962-1051), which bin/submatrices.py applies to every radial operator.
+ */
+int kore_gegenbauer_mult(int device, int N, const double *a0, double lam, int h, double *band);
 
 /* Number of kernels this library launched since load (for launch accounting). */
 int64_t kore_kernel_launches(void);

@@ -154,12 +154,40 @@ def mult_mat(a0, lam):
     return M
 
 
-class RadialOperators:
-    """The r^X D^Y operators of the two hydrodynamic sections for one (N, ricb)."""
+def mult_mat_gpu(a0, lam, device=0):
+    """``mult_mat`` computed on the GPU (``kore_gegenbauer_mult``): the same operator,
+    one thread per band entry."""
+    from . import _lib as L
+    a0 = np.ascontiguousarray(a0, dtype=np.float64)
+    N = a0.size
+    nz = np.nonzero(a0)[0]
+    if nz.size == 0:
+        return ss.csr_matrix((N, N))
+    h = min(int(nz.max()) + 1, N - 1)
+    band = np.zeros((2 * h + 1, N))
+    L.check(L.load().kore_gegenbauer_mult(int(device), N, L.ptr(a0), float(lam), h, L.ptr(band)),
+            "kore_gegenbauer_mult")
+    offs = np.arange(-h, h + 1)
+    # dia storage indexes column k of diagonal d; band is indexed by row j = k - d
+    data = np.zeros_like(band)
+    for i, d in enumerate(offs):
+        if d >= 0:
+            data[i, d:] = band[i, :N - d]
+        else:
+            data[i, :N + d] = band[i, -d:]
+    M = ss.dia_matrix((data, offs), shape=(N, N)).tocsr()
+    M.eliminate_zeros()
+    return M
 
-    def __init__(self, N, ricb, tol=1e-9):
+
+class RadialOperators:
+    """The r^X D^Y operators of the two hydrodynamic sections for one (N, ricb).
+    ``device``: compute the multiplication operators on that GPU (``mult_mat_gpu``)."""
+
+    def __init__(self, N, ricb, tol=1e-9, device=None):
         self.N = N
         self.ricb = ricb
+        self.device = device
         rp = [chebco(x, N, tol, ricb) for x in range(7)]
         S = [conv_mat(l, N) for l in range(4)]
         D = [None] + [diff_mat(l, N, ricb) for l in range(1, 5)]
@@ -177,7 +205,8 @@ class RadialOperators:
             return self._cache[key]
         g = 4 if section == "u" else 2
         a = self._Sto[dx] @ self._rp[rx]
-        M = self._G[g][g - dx] @ mult_mat(a, dx)
+        Mm = mult_mat(a, dx) if self.device is None else mult_mat_gpu(a, dx, self.device)
+        M = self._G[g][g - dx] @ Mm
         if dx > 0:
             M = M @ self._D[dx]
         M = ss.csr_matrix(M)
@@ -201,14 +230,15 @@ def boundary_values(x, N, nder, ricb, rcmb=RCMB):
 
 def hydro_pencil(m, symm, Ek, N, lmax, ricb=0.35, bci=1, bco=1, forcing=0, forcing_frequency=0.0,
                  forcing_amplitude_cmb=1.0, forcing_amplitude_icb=0.0, Gaspard=1.0, ViscosD=None,
-                 with_norm=False):
+                 with_norm=False, device=None):
     """(A, B) as bin/assemble.py writes them for the hydrodynamic shell problem.
 
     forcing == 0: eigenproblem, B is the (sizmat x sizmat) float64 matrix, A and B
     divided by ||B||_F (with_norm=True also returns that norm).  forcing in (7, 9, 10):
     forced problem, A = i w u + Coriolis - viscous (unnormalised) and B is the
     (sizmat x 1) forcing column.  The forced matrix at frequency w is therefore
-    ||B||_F (A_eig - i w B_eig) of the eigen pencil.
+    ||B||_F (A_eig - i w B_eig) of the eigen pencil.  ``device``: build the Gegenbauer
+    multiplication operators on that GPU instead of the host.
     """
     if ricb <= 0:
         raise ValueError("only the spherical shell (ricb > 0) is assembled here")
@@ -219,7 +249,7 @@ def hydro_pencil(m, symm, Ek, N, lmax, ricb=0.35, bci=1, bco=1, forcing=0, forci
     nb = (lmax - m + 1) // 2
     lp, lt = ell(m, lmax, symm)
     wf = forcing_frequency if forcing else 0.0
-    R = RadialOperators(N, ricb)
+    R = RadialOperators(N, ricb, device=device)
     op = R.op
     lp_f = lp.astype(float)
     lt_f = lt.astype(float)

@@ -203,6 +203,8 @@ int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol, u
                        const double *shift_tols = nullptr);
 int kore_ir_reset(kore_plan *p);
 int kore_ir_read(kore_plan *p, IrState *out);
+// once per plan, before the sparse products run: their launch attributes
+int kore_spmv_prepare(kore_plan *p);
 // y = B x on padded vectors
 int kore_spmv_b(kore_plan *p, const double2 *x, double2 *y);
 // y_s = B x_s for the factorised shifts s in live_mask (vectors at offset s * np)

@@ -278,6 +278,7 @@ int create(const kore_pencil_desc *d, int device, kore_plan **out) {
     kore_build_levels(p);
     KORE_CUDA_TRY(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
     KORE_CUDA_TRY(cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, device));
+    KORE_TRY(kore_spmv_prepare(p));
 
     std::vector<int> rowlen;
     {

@@ -543,6 +543,7 @@ constexpr int kRowUnroll = 4;
 
 struct SpmvArgs {
     int64_t np;
+    int S, K;               // padded block size, blocks: row p's columns lie in blocks p/S - 1 .. p/S + 1
     int mode;               // 0: y = B x.  1: y = A x - lam B x.  2: y = b - (A x - lam B x)
     int has_b;
     const int *srow, *smid, *scol;  // A split into real and imaginary coefficients (kore_plan::d_s*)
@@ -562,11 +563,24 @@ struct SpmvArgs {
     unsigned live_mask;     // shift s (< 32) is computed only when bit s is set
 };
 
+// The entries of x one CTA of short rows reads, staged in shared memory: columns
+// [w0, w1) (block-aligned: the blocks of the CTA's rows and one on either side).  An
+// entry outside the window (none for a plan, whose band check keeps every column in the
+// neighbouring blocks) is read from global memory.
+struct XWin {
+    const double2 *__restrict__ sh;
+    int64_t w0, w1;
+    __device__ __forceinline__ double2 get(const double2 *__restrict__ x, int c) const {
+        return (c >= w0 && c < w1) ? sh[c - w0] : __ldg(x + c);
+    }
+};
+
 // acc += sum over the values sub, sub + LANES, ... of [e0, e1) of val[e] x[col[e]]
-// (kRowUnroll loads in flight per lane, two FP64 multiply-adds per value)
-template <int LANES>
+// (kRowUnroll loads in flight per lane, two FP64 multiply-adds per value); x entries from
+// the window when one is given
+template <int LANES, bool WIN>
 __device__ __forceinline__ void seg_dot(const int *__restrict__ col, const double *__restrict__ val, int e0, int e1,
-                                        int sub, const double2 *__restrict__ x, double2 &acc) {
+                                        int sub, const double2 *__restrict__ x, const XWin &xw, double2 &acc) {
     for (int e = e0 + sub; e < e1; e += LANES * kRowUnroll) {
         int c[kRowUnroll];
         double v[kRowUnroll];
@@ -579,7 +593,7 @@ __device__ __forceinline__ void seg_dot(const int *__restrict__ col, const doubl
 #pragma unroll
         for (int u = 0; u < kRowUnroll; ++u)
             if (c[u] >= 0) {
-                const double2 xv = __ldg(x + c[u]);
+                const double2 xv = WIN ? xw.get(x, c[u]) : __ldg(x + c[u]);
                 acc.x = fma(v[u], xv.x, acc.x);
                 acc.y = fma(v[u], xv.y, acc.y);
             }
@@ -588,16 +602,19 @@ __device__ __forceinline__ void seg_dot(const int *__restrict__ col, const doubl
 
 // Partial sums of row p: the real-coefficient values of A (sr), its imaginary-coefficient
 // values (si: A x = sr + i si) and B (sb).
-template <int LANES>
+template <int LANES, bool WIN>
 __device__ __forceinline__ void row_dot(const SpmvArgs &a, int64_t p, int sub, const double2 *__restrict__ x,
-                                        double2 &sr, double2 &si, double2 &sb) {
+                                        const XWin &xw, double2 &sr, double2 &si, double2 &sb) {
     if (a.mode != 0) {
         const int em = a.smid[p];
-        seg_dot<LANES>(a.scol, a.sval, a.srow[p], em, sub, x, sr);
-        seg_dot<LANES>(a.scol, a.sval, em, a.srow[p + 1], sub, x, si);
+        seg_dot<LANES, WIN>(a.scol, a.sval, a.srow[p], em, sub, x, xw, sr);
+        seg_dot<LANES, WIN>(a.scol, a.sval, em, a.srow[p + 1], sub, x, xw, si);
     }
-    if (a.has_b) seg_dot<LANES>(a.bcol, a.bval, a.brow[p], a.brow[p + 1], sub, x, sb);
+    if (a.has_b) seg_dot<LANES, WIN>(a.bcol, a.bval, a.brow[p], a.brow[p + 1], sub, x, xw, sb);
 }
+
+// x entries of the window of a CTA of 256 short rows: at most (255 / S + 4) blocks
+__host__ __device__ __forceinline__ int64_t spmv_window(int S) { return (int64_t)(255 / S + 4) * S; }
 
 // |v| of a double as the bits of its absolute value: for non-negative IEEE doubles the
 // integer order is the numeric order, so maxima run on the integer units, not on the
@@ -611,6 +628,7 @@ __device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long v
 }
 
 __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
+    extern __shared__ double2 xsh[];   // spmv_window(S) entries
     const int64_t s = blockIdx.y;
     if (!mask_has(a.live_mask, s) || (a.skip && a.skip[s * a.skip_stride])) return;
     const int64_t np = a.np;
@@ -632,7 +650,16 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
     };
     if ((int)blockIdx.x < a.short_blocks) {
         static_assert(kRowLanes == 1, "one thread per short row");
-        const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+        // stage the x entries of the blocks this CTA's rows couple to (coalesced), so the
+        // rows' gathers hit shared memory instead of waiting on L2
+        const int64_t r0 = blockIdx.x * (int64_t)blockDim.x;
+        const int64_t rl = ((r0 + blockDim.x < np) ? r0 + blockDim.x : np) - 1;
+        const int64_t b0 = (r0 / a.S > 0) ? r0 / a.S - 1 : 0;
+        const int64_t b1 = (rl / a.S + 1 < a.K) ? rl / a.S + 1 : a.K - 1;
+        XWin xw{xsh, b0 * a.S, (b1 + 1) * a.S};
+        for (int64_t c = xw.w0 + threadIdx.x; c < xw.w1; c += blockDim.x) xsh[c - xw.w0] = __ldg(x + c);
+        __syncthreads();
+        const int64_t p = r0 + threadIdx.x;
         bool live = p < np;
         if (live) {
             const int len = (a.srow[p + 1] - a.srow[p]) + (a.has_b ? a.brow[p + 1] - a.brow[p] : 0);
@@ -640,7 +667,7 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
         }
         if (live) {
             double2 sr = mk(0.0, 0.0), si = mk(0.0, 0.0), sb = mk(0.0, 0.0);
-            row_dot<1>(a, p, 0, x, sr, si, sb);
+            row_dot<1, true>(a, p, 0, x, xw, sr, si, sb);
             finish(p, sr, si, sb);
         }
     } else {
@@ -649,7 +676,7 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs a) {
         if (wid < a.nlong) {
             const int64_t p = a.long_rows[wid];
             double2 sr = mk(0.0, 0.0), si = mk(0.0, 0.0), sb = mk(0.0, 0.0);
-            row_dot<32>(a, p, lane, x, sr, si, sb);
+            row_dot<32, false>(a, p, lane, x, XWin{nullptr, 0, 0}, sr, si, sb);
             sr = warp_sum(sr);
             si = warp_sum(si);
             sb = warp_sum(sb);
@@ -782,10 +809,11 @@ int absmax(kore_plan *p, const double2 *v, double *out, double *scratch) {
 // CTAs of one sparse product: the 4-lane part, then 8 long rows per CTA
 unsigned spmv_short_blocks(int64_t np) { return kore_div_up(np * kRowLanes, 256); }
 unsigned spmv_grid(const kore_plan *p) { return spmv_short_blocks(p->np) + kore_div_up(p->nlong, 8); }
+size_t spmv_smem(const kore_plan *p) { return (size_t)spmv_window(p->S) * sizeof(double2); }
 
 SpmvArgs spmv_args(const kore_plan *p, int mode, const double2 *x, double2 *y) {
     SpmvArgs a;
-    a.np = p->np; a.mode = mode; a.has_b = p->has_b ? 1 : 0;
+    a.np = p->np; a.S = p->S; a.K = p->K; a.mode = mode; a.has_b = p->has_b ? 1 : 0;
     a.srow = p->d_srow; a.smid = p->d_smid; a.scol = p->d_scol; a.sval = p->d_sval;
     a.brow = p->d_brow; a.bcol = p->d_bcol; a.bval = p->d_bval;
     a.long_rows = p->d_long_rows; a.nlong = p->nlong; a.short_blocks = (int)spmv_short_blocks(p->np);
@@ -798,10 +826,15 @@ SpmvArgs spmv_args(const kore_plan *p, int mode, const double2 *x, double2 *y) {
 
 }  // namespace
 
+int kore_spmv_prepare(kore_plan *p) {
+    // the x window of a CTA exceeds the default 48 KB of shared memory for S > 760
+    return kore_allow_max_dyn_smem(k_spmv, p->device);
+}
+
 int kore_spmv_b(kore_plan *p, const double2 *x, double2 *y) {
     if (!p->has_b) return KORE_EINVAL;
     if (p->prof) KORE_TRY(kore_prof_mark(p, 2, true));
-    k_spmv<<<spmv_grid(p), 256, 0, p->stream>>>(spmv_args(p, 0, x, y));
+    k_spmv<<<spmv_grid(p), 256, spmv_smem(p), p->stream>>>(spmv_args(p, 0, x, y));
     KORE_LAUNCHED(1);
     if (p->prof) KORE_TRY(kore_prof_mark(p, 2, false));
     KORE_CUDA_TRY(cudaGetLastError());
@@ -813,7 +846,7 @@ int kore_spmv_b_shifts(kore_plan *p, const double2 *x, double2 *y, unsigned live
     if (p->prof) KORE_TRY(kore_prof_mark(p, 2, true));
     SpmvArgs a = spmv_args(p, 0, x, y);
     a.live_mask = live_mask;
-    k_spmv<<<dim3(spmv_grid(p), std::max(1, p->nshift)), 256, 0, p->stream>>>(a);
+    k_spmv<<<dim3(spmv_grid(p), std::max(1, p->nshift)), 256, spmv_smem(p), p->stream>>>(a);
     KORE_LAUNCHED(1);
     if (p->prof) KORE_TRY(kore_prof_mark(p, 2, false));
     KORE_CUDA_TRY(cudaGetLastError());
@@ -825,7 +858,7 @@ int kore_spmv_a_shifts(kore_plan *p, const double2 *x, double2 *y, unsigned live
     SpmvArgs a = spmv_args(p, 1, x, y);   // A x - 0 B x
     a.has_b = 0;
     a.live_mask = live_mask;
-    k_spmv<<<dim3(spmv_grid(p), std::max(1, p->nshift)), 256, 0, p->stream>>>(a);
+    k_spmv<<<dim3(spmv_grid(p), std::max(1, p->nshift)), 256, spmv_smem(p), p->stream>>>(a);
     KORE_LAUNCHED(1);
     if (p->prof) KORE_TRY(kore_prof_mark(p, 2, false));
     KORE_CUDA_TRY(cudaGetLastError());
@@ -835,7 +868,7 @@ int kore_spmv_a_shifts(kore_plan *p, const double2 *x, double2 *y, unsigned live
 int kore_spmv_pencil(kore_plan *p, double lre, double lim, const double2 *x, double2 *y) {
     SpmvArgs a = spmv_args(p, 1, x, y);
     a.lam = mk(lre, lim);
-    k_spmv<<<spmv_grid(p), 256, 0, p->stream>>>(a);
+    k_spmv<<<spmv_grid(p), 256, spmv_smem(p), p->stream>>>(a);
     KORE_LAUNCHED(1);
     KORE_CUDA_TRY(cudaGetLastError());
     return KORE_OK;
@@ -973,7 +1006,7 @@ int kore_apply_inverse(kore_plan *p, const double2 *b, double2 *x, double tol, u
     ra.live_mask = live_mask;
     for (int it = 0; it < kIrMax; ++it) {
         if (p->prof) KORE_TRY(kore_prof_mark(p, 2, true));
-        k_spmv<<<dim3(grid, ns), 256, 0, p->stream>>>(ra);
+        k_spmv<<<dim3(grid, ns), 256, spmv_smem(p), p->stream>>>(ra);
         k_ir_check<<<ns, 1024, 0, p->stream>>>(p->d_part, (int)grid, bn, p->d_minf, tol, tols, p->d_ir, rn);
         KORE_LAUNCHED(2);
         if (p->prof) KORE_TRY(kore_prof_mark(p, 2, false));
@@ -1102,7 +1135,7 @@ int noalloc_solve(kore_plan *p, NoAllocScratch *s, const double2 *b_dev, double2
         SpmvArgs ra = spmv_args(p, 2, s->xp, s->r);
         ra.lam = mk(p->sigma_re, p->sigma_im); ra.rhs = s->bp; ra.part = s->part; ra.skip = &s->ir.done;
         for (int it = 0; it < kIrMax; ++it) {
-            k_spmv<<<grid, 256, 0, st>>>(ra);
+            k_spmv<<<grid, 256, spmv_smem(p), st>>>(ra);
             k_ir_check<<<1, 1024, 0, st>>>(s->part, (int)grid, bn, p->d_minf, tol, ShiftTols{}, &s->ir, rn);
             KORE_LAUNCHED(2);
             KORE_TRY(noalloc_sweep<float2>(p, s, s->r, rn, s->xp, 1, &s->ir.done, st));

@@ -363,6 +363,9 @@ class EPS:
 
     def solve(self):
         p = self.pencil
+        if self.which not in ("TM", "TR", "TI"):
+            # SLEPc's EPSSetUp stops here under -st_type sinvert, the kore path's transformation
+            raise ValueError(f"shift-and-invert requires a target 'which' (TM, TR or TI), not {self.which!r}")
         if p.sigma != self.target or p.precision != self.precision:
             p.factor(self.target, self.precision)
         nev, ncv, _ = self.getDimensions()

@@ -93,7 +93,8 @@ def test_fullsize_batched_targets(gpu_lib, shell2, fp64_measurements):
         res = eigs_targets(p, targets, 16, "TM", "mixed", seeds=[5, 6, 7, 8])
     for (lam, X, st), tau in zip(res, targets):
         assert len(lam) >= 16, (tau, st)
-        assert cd.rel_residuals(A, B, lam[:16], X[:, :16]).max() <= max(4.0 * float(np.max(ref_res[:16])), 1e-16)
+        # the FP64 path's residuals range from 2e-17 to 1e-16 over these targets
+        assert cd.rel_residuals(A, B, lam[:16], X[:, :16]).max() <= 2e-16, tau
     lam, X, _ = res[0]
     r = cd.compare(A, B, 0.5j, 16, lam, X, ref, ref_res, band, sets)
     assert r["within_band"] == 16 and r["in_window"] == 16, r

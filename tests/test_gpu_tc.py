@@ -32,3 +32,31 @@ def test_mixed_factor_needs_few_corrections(gpu_lib, case):
         x, st = p.solve(b, refine_tol=1e-14, stats=True)
     assert solve_residual((A - 0.37j * B).tocsr(), x, b) < 1e-14
     assert st["refine_iters_max"] <= 3, st
+
+
+def test_gegenbauer_mult_matches_host(gpu_lib):
+    """The GPU multiplication operators (kore_gegenbauer_mult) against the host ones,
+    which tests/test_assembly.py pins to the reference's Mlam through its matrices: the
+    r^X coefficients converted to C^(Y) for every operator the hydro assembly uses, at
+    N = 48 and N = 400."""
+    import numpy as np
+    from kore_gb300.assembly import RadialOperators, mult_mat, mult_mat_gpu
+    for N in (48, 400):
+        R = RadialOperators(N, 0.35)
+        for rx in range(7):
+            for dx in range(5):
+                a = R._Sto[dx] @ R._rp[rx]
+                Mh, Mg = mult_mat(a, dx), mult_mat_gpu(a, dx)
+                ref = abs(Mh).max()
+                assert abs(Mh - Mg).max() <= 1e-13 * max(ref, 1e-300), (N, rx, dx)
+
+
+def test_hydro_pencil_with_gpu_operators(gpu_lib):
+    """The whole hydro pencil assembled with the GPU multiplication operators equals the
+    host-assembled one."""
+    import numpy as np
+    from kore_gb300.assembly import hydro_pencil
+    A, B = hydro_pencil(1, 1, 1e-4, 48, 40, 0.35)
+    Ag, Bg = hydro_pencil(1, 1, 1e-4, 48, 40, 0.35, device=0)
+    assert abs(A - Ag).max() <= 1e-13 * abs(A).max()
+    assert abs(B - Bg).max() == 0.0
