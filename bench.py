@@ -56,12 +56,15 @@ FORCED = {
 SWEEP_TRAFFIC_RATIO = 542.4 / 551.7
 
 
+def describe_forced(c):
+    return (f"batched forced solves: hydro shell ricb={c['ricb']} no-slip m={c['m']} symm={c['symm']} "
+            f"Ek={c['Ek']:g} N={c['N']} lmax={c['lmax']}, forcing 10, {c['nfreq']} frequencies in [-2, 2] "
+            f"({c['group']} per batch), plus {c['instances']} uneven instances")
+
+
 def describe(w):
     if w in FORCED:
-        c = FORCED[w]
-        return (f"batched forced solves: hydro shell ricb={c['ricb']} no-slip m={c['m']} symm={c['symm']} "
-                f"Ek={c['Ek']:g} N={c['N']} lmax={c['lmax']}, forcing 10, {c['nfreq']} frequencies in [-2, 2] "
-                f"({c['group']} per batch), plus {c['instances']} uneven instances")
+        return describe_forced(FORCED[w])
     m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[w]
     return (f"hydro shell ricb={ricb} no-slip m={m} symm={symm} Ek={Ek:g} N={N} lmax={lmax}, "
             f"target {tau.imag:g}i, nev={nev}, which={which}")
@@ -314,10 +317,11 @@ def uneven_instances(count, seed=7):
     return out
 
 
-def forced_bench(args, local):
+def forced_bench(args, local, c=None, emit=True):
     """Batched forced solves: forced solves/s, mixed (complex64 batched factorisation +
     FP64 refinement) against the FP64 GPU path, through the public Python API
-    (kore_gb300.forced_sweep: host right-hand sides in, host solutions out)."""
+    (kore_gb300.forced_sweep: host right-hand sides in, host solutions out).  Prints the
+    JSON line (emit) and returns it."""
     import torch
     import scipy.sparse as ss
     from concurrent.futures import ThreadPoolExecutor
@@ -327,7 +331,7 @@ def forced_bench(args, local):
     from kore_gb300.structure import layout_from_params
     kb.build()
     torch.cuda.set_device(local)
-    c = FORCED[args.workload]
+    c = c or FORCED[args.workload]
     geo = dict(m=c["m"], symm=c["symm"], Ek=c["Ek"], N=c["N"], lmax=c["lmax"], ricb=c["ricb"])
     Ae, Be, nrm = hydro_pencil(geo["m"], geo["symm"], geo["Ek"], geo["N"], geo["lmax"], geo["ricb"], with_norm=True)
     b = forcing_vector(geo["m"], geo["symm"], geo["N"], geo["lmax"], geo["ricb"], 10).toarray().ravel()
@@ -393,7 +397,7 @@ def forced_bench(args, local):
         "value": value, "unit": "solves/s", "n_gpus": 1, "steps": len(gt), "warmup": max(args.warmup, 1),
         "ms_per_step": 1e3 * wall / len(gt), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64 factor + f64 refinement", "data": "synthetic: pencil assembled from the kore parameters",
-        "config": {"workload": describe(args.workload), "n": n, "blocks": int(lay.nblocks),
+        "config": {"workload": describe_forced(c), "n": n, "blocks": int(lay.nblocks),
                    "block": int(lay.block_sizes.max()), "batch": G, "l2": "inputs larger than L2",
                    "parallelism": "replicas x1"},
         "latency_ms": {"batch_p50": 1e3 * float(np.percentile(gt, 50)), "batch_p99": 1e3 * float(np.percentile(gt, 99))},
@@ -409,7 +413,9 @@ def forced_bench(args, local):
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": hbytes[0] // len(gt),
                 "d2h_bytes_per_step": hbytes[1] // len(gt)},
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 # Serving: a seeded Poisson stream of requests over a pool of pencils drawn from the
@@ -418,6 +424,8 @@ def forced_bench(args, local):
 # shift i*U[-2, 2]), at each arrival rate in `rates` (requests/s).
 SERVE = {
     "serve5": dict(pool=8, requests=120, rates=(2.0, 6.0), workers=4),
+    # the summary carried on the headline line: one arrival rate
+    "serve5h": dict(pool=8, requests=120, rates=(3.0,), workers=4),
     "serve5s": dict(pool=3, requests=24, rates=(4.0,), workers=3, small=True),
 }
 
@@ -435,9 +443,10 @@ def serve_pool(count, seed=11, small=False):
     return out
 
 
-def serve_bench(args, local):
+def serve_bench(args, local, c=None, emit=True):
     """Serving queue (kore_gb300.serve.Server): p50/p99 request latency and throughput of
-    a Poisson request stream at several arrival rates."""
+    a Poisson request stream at several arrival rates.  Prints the JSON line (emit) and
+    returns it."""
     import torch
     from kore_gb300 import build as kb
     from kore_gb300.assembly import forcing_vector, hydro_params, hydro_pencil
@@ -445,7 +454,7 @@ def serve_bench(args, local):
     from kore_gb300.structure import layout_from_params
     kb.build()
     torch.cuda.set_device(local)
-    c = SERVE[args.workload]
+    c = c or SERVE[args.workload]
     pool = []
     for d in serve_pool(c["pool"], small=c.get("small", False)):
         A, B, nrm = hydro_pencil(d["m"], 1, d["Ek"], d["N"], d["lmax"], d["ricb"], with_norm=True)
@@ -493,6 +502,7 @@ def serve_bench(args, local):
         per_rate.append({"arrival_rate": rate, "requests": len(reqs), "ok": ok, "eigen_short_of_nev": short,
                          "throughput": len(reqs) / wall, "p50_ms": float(np.percentile(lat, 50)),
                          "p99_ms": float(np.percentile(lat, 99)), "factor_cache_hits": st["factor_cache_hits"],
+                         "joined_running_engine": st["joined_running_engine"],
                          "plans_created": st["plans_created"], "plans_evicted": st["plans_evicted"]})
     best = max(per_rate, key=lambda r: r["throughput"])
     line = {
@@ -508,7 +518,9 @@ def serve_bench(args, local):
                    "parallelism": "replicas x1"},
         "rates": per_rate,
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
@@ -522,6 +534,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--no-forced", action="store_true", help="leave the batched forced-solve summary out")
+    ap.add_argument("--no-serve", action="store_true", help="leave the serving summary out")
     ap.add_argument("--batch", type=int, default=4, help="targets of the batched form (1: skip it)")
     args = ap.parse_args()
 
@@ -651,6 +665,13 @@ def main():
         e2e = {"value": nev / (np.mean(ev_ms) / 1e3), "unit": "eigenpairs/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(ev_ms))}
 
+    # ---- configs 4 and 5 on the same line (their own sizes are in their config keys)
+    forced = serve = None
+    if rank == 0 and not args.no_forced:
+        forced = forced_bench(args, local, FORCED["forced4"], emit=False)
+    if rank == 0 and not args.no_serve:
+        serve = serve_bench(args, local, SERVE["serve5h"], emit=False)
+
     if rank != 0:
         return
     hbm, _, src = peaks()
@@ -694,6 +715,10 @@ def main():
                                                                             "ortho_ms", "schur_ms")}},
         "clocks": clocks.summary(),
         "e2e": e2e,
+        "forced_sweep": forced and {k: forced[k] for k in ("metric", "value", "unit", "config", "latency_ms",
+                                                           "max_resid", "fp64", "speedup_vs_fp64", "uneven",
+                                                           "gpu_launches", "e2e")},
+        "serving": serve and {k: serve[k] for k in ("metric", "value", "unit", "config", "rates")},
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)

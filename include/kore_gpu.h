@@ -240,9 +240,14 @@ int kore_plan_estimate_bytes(const kore_pencil_desc *desc, int precision, int ns
  *    freed oldest first to make room.  Requests start in arrival order, except that one
  *    which does not fit yet does not hold back later ones that do (until it has waited
  *    longer than 200 ms, after which nothing new starts before it).
+ *  - Continuous batching: eigen requests with the same non-zero pencil_key and
+ *    precision run together in the factor slots of one plan (the engine of
+ *    kore_eigs_shifts, four slots), sharing every launch; one that arrives while others
+ *    of its pencil run takes the next free slot instead of starting a plan of its own.
  *  - Factor cache: requests with the same non-zero pencil_key share uploaded plans; a
- *    request whose (key, shift, precision) matches an idle cached plan skips the
- *    upload and the factorisation.  pencil_key = 0: the plan is freed after the request.
+ *    forced request whose (key, shift, precision) matches an idle cached plan skips the
+ *    factorisation, and an eigen request reuses a slot that still holds its target's
+ *    factors.  pencil_key = 0: the plan is freed after the request.
  *  - The caller keeps the pencil arrays, the right-hand side and the output buffers
  *    alive until kore_batch_poll reports the request finished.
  *  - A result does not depend on what else is running: each request runs on its own
@@ -280,8 +285,9 @@ int kore_batch_submit(kore_batch *batch, const kore_request *req, uint64_t *tick
  * released), KORE_EPENDING when it has not after wait_ms milliseconds (-1: wait).
  */
 int kore_batch_poll(kore_batch *batch, uint64_t ticket, int wait_ms, int *status);
-/* out[8]: submitted, finished, running, queued, device bytes in plans, factor-cache
- * hits, plans created, plans freed to make room */
+/* out[9]: submitted, finished, running, queued, device bytes in plans, factor-cache
+ * hits, plans created, plans freed to make room, eigen requests that joined a running
+ * engine */
 int kore_batch_stats(kore_batch *batch, int64_t *out);
 /* Waits for running requests, cancels queued ones (KORE_ECANCELLED), frees all plans. */
 int kore_batch_destroy(kore_batch *batch);

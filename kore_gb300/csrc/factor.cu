@@ -888,3 +888,25 @@ int kore_factor_slot(kore_plan *p, int slot, double sigma_re, double sigma_im) {
     p->factored = true;
     return KORE_OK;
 }
+
+int kore_factor_reserve(kore_plan *p, int nslot, int precision) {
+    if (nslot <= 0 || (precision != KORE_PREC_FP64 && precision != KORE_PREC_MIXED)) return KORE_EINVAL;
+    const size_t elt = (precision == KORE_PREC_FP64) ? sizeof(double2) : sizeof(float2);
+    p->factored = false;
+    KORE_TRY(ensure_factor_storage(p, nslot, elt));
+    p->prec = precision;
+    p->nshift = nslot;
+    p->fw_lo = 0;
+    p->fw_n = nslot;
+    // no slot holds a shift yet (NaN matches no target)
+    p->sigmas.assign(nslot, mk(NAN, NAN));
+    p->minfs.assign(nslot, 0.0);
+    p->sigma_re = p->sigma_im = NAN;
+    KORE_CUDA_TRY(cudaMemcpyAsync(p->d_sigma, p->sigmas.data(), nslot * sizeof(double2), cudaMemcpyHostToDevice,
+                                  p->stream));
+    KORE_CUDA_TRY(cudaMemcpyAsync(p->d_minf, p->minfs.data(), nslot * sizeof(double), cudaMemcpyHostToDevice,
+                                  p->stream));
+    KORE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    p->factored = true;   // slot by slot from here (kore_factor_slot)
+    return KORE_OK;
+}

@@ -220,6 +220,38 @@ int kore_gather_shifts(kore_plan *p, const double2 *orig, double2 *padded);
 int kore_scatter_shifts(kore_plan *p, const double2 *padded, double2 *orig);
 
 // eigs.cu
-// ntarget Krylov-Schur runs, target t around factorised shift t (ntarget = nshift)
+// ntarget Krylov-Schur runs, targets 0 .. nshift-1 around the factorised shifts, the
+// others admitted into slots as earlier ones finish
 int kore_eigs_impl(kore_plan *p, int ntarget, const kore_eps_opts *o, double *evals, double *evecs,
                    int max_pairs, int *nconv, kore_stats *st);
+
+// One target of the batched eigensolve engine: its options and where its results go.
+struct EigsTarget {
+    kore_eps_opts opts{};
+    double *evals = nullptr;       // 2 * max_pairs doubles
+    double *evecs = nullptr;       // NULL or 2 * n * max_pairs doubles
+    int max_pairs = 0;
+    int *nconv = nullptr;
+    kore_stats *stats = nullptr;   // may be NULL
+    void *tag = nullptr;           // the source's handle of the target
+    int reused = 0;                // set by the engine: the slot already held this shift's factors
+};
+// Supplier of targets to kore_eigs_engine (called from the engine's thread).
+struct EigsSource {
+    // a target for a free slot, or false when there is none now
+    virtual bool next(EigsTarget *t) = 0;
+    // the target's results are written; status KORE_OK, KORE_ENOCONV, KORE_ENAN or the
+    // error that ended it
+    virtual void finished(const EigsTarget &t, int status) = 0;
+    virtual ~EigsSource() = default;
+};
+// Runs Krylov-Schur solves in the plan's nshift factor slots until every slot is idle
+// and the source has nothing more.  Slot s holds a usable factorisation of shift
+// sigmas[s] when valid[s] (may be null: none; on return, the slots' state); a target is
+// placed in a free slot that holds its shift if there is one, else its shift is
+// factorised in a free slot.  Slots hold bases of max_ncv + 1 vectors; a target with a
+// larger ncv is handed back with KORE_EINVAL.
+int kore_eigs_engine(kore_plan *p, EigsSource *src, bool *valid, int max_ncv);
+// factor storage for nslot shifts in `precision`, none factorised yet: the slots of
+// kore_eigs_engine
+int kore_factor_reserve(kore_plan *p, int nslot, int precision);

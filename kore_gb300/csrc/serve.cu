@@ -25,15 +25,25 @@ double ms_since(Clock::time_point a, Clock::time_point b) {
     return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
-// A plan of one pencil, idle in the cache or in use by one request.
+// Eigen slots of a shared plan: eigen requests of one pencil run together in the
+// batched engine (kore_eigs_engine), up to this many at a time.
+constexpr int kServeSlots = 4;
+
+// A plan of one pencil, idle in the cache or in use by one request (forced) or by the
+// eigen engine (eigen requests of its pencil).
 struct CachedPlan {
     uint64_t key = 0;
     kore_plan *plan = nullptr;
     int64_t bytes = 0;          // charged against the budget (estimate, then the larger of it and the plan's own count)
     bool busy = false;
-    bool factored = false;
+    bool engine = false;        // busy running the eigen engine: new eigen requests of this key join it
+    bool factored = false;      // one shift factorised (forced requests)
     double sre = 0, sim = 0;
     int prec = -1;
+    int slots = 0;              // eigen slots reserved (kore_factor_reserve), 0 if the plan holds one shift
+    int slot_prec = -1;         // precision of the reserved slots
+    int engine_prec = -1;       // precision of the running engine
+    bool slot_valid[kServeSlots] = {};
     uint64_t last_use = 0;
 };
 
@@ -43,6 +53,7 @@ struct Request {
     Clock::time_point t_submit, t_start, t_end;
     int status = KORE_EPENDING;
     bool done = false;
+    bool by_engine = false;     // started and finished by an eigen engine's source
     int64_t est = -1;           // estimate of a new plan for this request
 };
 
@@ -61,17 +72,22 @@ struct kore_batch {
     bool stop = false;
     uint64_t next_ticket = 1, clock = 0;
     int64_t submitted = 0, finished = 0, running = 0, hits = 0, created = 0, evicted = 0;
+    int64_t joined = 0;         // eigen requests admitted into a running engine's free slot
 };
 
 namespace {
 
 constexpr double kHoldBackMs = 200.0;   // a request waiting longer than this blocks new starts
 
+// Largest ncv an engine slot holds (the engine's basis size).
+constexpr int kServeMaxNcv = 64;
+
+bool shared_eigen(const kore_request &r) { return r.kind == KORE_REQ_EIGEN && r.pencil_key != 0; }
+
 int estimate(const kore_request &r, int64_t *bytes) {
-    const int ncv = (r.kind == KORE_REQ_EIGEN)
-                        ? (r.opts.ncv > 0 ? r.opts.ncv : std::max(2 * r.opts.nev, r.opts.nev + 15))
-                        : 0;
-    return kore_plan_estimate_bytes(r.pencil, r.precision, 1, ncv, bytes);
+    if (r.kind == KORE_REQ_EIGEN)
+        return kore_plan_estimate_bytes(r.pencil, r.precision, shared_eigen(r) ? kServeSlots : 1, kServeMaxNcv, bytes);
+    return kore_plan_estimate_bytes(r.pencil, r.precision, 1, 0, bytes);
 }
 
 // An idle plan of this key factorised at this shift and precision, else an idle plan of
@@ -82,7 +98,8 @@ CachedPlan *find_idle(kore_batch *b, const kore_request &r, bool *hit) {
     CachedPlan *any = nullptr;
     for (auto &c : b->plans) {
         if (c->busy || c->key != r.pencil_key) continue;
-        if (c->factored && c->prec == r.precision && c->sre == r.sigma_re && c->sim == r.sigma_im) {
+        if (r.kind == KORE_REQ_FORCED && c->factored && c->prec == r.precision && c->sre == r.sigma_re &&
+            c->sim == r.sigma_im) {
             *hit = true;
             return c.get();
         }
@@ -109,11 +126,22 @@ bool make_room(kore_batch *b, int64_t need) {
     return true;
 }
 
+// True when an engine of this request's pencil and precision is running.  Caller holds
+// the lock.
+bool engine_running(kore_batch *b, const kore_request &r) {
+    for (auto &c : b->plans)
+        if (c->engine && c->key == r.pencil_key && c->engine_prec == r.precision) return true;
+    return false;
+}
+
 // Pick the next request that can start and reserve its plan.  Caller holds the lock.
 Request *admit(kore_batch *b, CachedPlan **slot) {
     const auto now = Clock::now();
     for (auto it = b->queue.begin(); it != b->queue.end(); ++it) {
         Request *q = *it;
+        // an eigen request of a pencil whose engine is running joins that engine when a
+        // slot frees up; it does not start on a second plan
+        if (shared_eigen(q->r) && engine_running(b, q->r)) continue;
         bool hit = false;
         CachedPlan *c = find_idle(b, q->r, &hit);
         if (c) {
@@ -155,12 +183,109 @@ Request *admit(kore_batch *b, CachedPlan **slot) {
     return nullptr;
 }
 
+// Requests for the eigen engine of one plan: the admitted request first, then queued
+// eigen requests of the same pencil and precision as slots free up.
+struct ServeSource : EigsSource {
+    kore_batch *b;
+    CachedPlan *c;
+    Request *first;
+    bool gave_first = false;
+    static void fill(Request *q, EigsTarget *t) {
+        const kore_request &r = q->r;
+        t->opts = r.opts;
+        t->opts.target_re = r.sigma_re;
+        t->opts.target_im = r.sigma_im;
+        t->evals = r.evals;
+        t->evecs = r.evecs;
+        t->max_pairs = r.max_pairs;
+        t->nconv = r.nconv;
+        t->stats = nullptr;
+        t->tag = q;
+    }
+    bool next(EigsTarget *t) override {
+        if (!gave_first) {
+            gave_first = true;
+            fill(first, t);
+            return true;
+        }
+        std::lock_guard<std::mutex> lk(b->mu);
+        if (b->stop) return false;
+        for (auto it = b->queue.begin(); it != b->queue.end(); ++it) {
+            Request *q = *it;
+            if (!shared_eigen(q->r) || q->r.pencil_key != c->key || q->r.precision != c->engine_prec) continue;
+            if (!q->r.evals || !q->r.nconv || q->r.max_pairs <= 0) continue;   // left to a worker (EINVAL)
+            b->queue.erase(it);
+            q->t_start = Clock::now();
+            q->by_engine = true;
+            ++b->running;
+            ++b->joined;
+            fill(q, t);
+            return true;
+        }
+        return false;
+    }
+    void finished(const EigsTarget &t, int status) override {
+        Request *q = static_cast<Request *>(t.tag);
+        if (t.reused) {
+            std::lock_guard<std::mutex> lk(b->mu);
+            ++b->hits;
+        }
+        if (q == first) {   // the worker finishes the request it admitted
+            first->status = status;
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lk(b->mu);
+            q->t_end = Clock::now();
+            q->status = status;
+            q->done = true;
+            --b->running;
+            ++b->finished;
+            if (q->r.timing_ms) {
+                q->r.timing_ms[0] = ms_since(q->t_submit, q->t_start);
+                q->r.timing_ms[1] = ms_since(q->t_start, q->t_end);
+                q->r.timing_ms[2] = ms_since(q->t_submit, q->t_end);
+            }
+        }
+        b->cv_done.notify_all();
+    }
+};
+
 int run_request(kore_batch *b, Request *q, CachedPlan *c) {
     const kore_request &r = q->r;
     if (!c->plan) {
         KORE_TRY(kore_plan_create(r.pencil, b->device, &c->plan));
         std::lock_guard<std::mutex> lk(b->mu);
         ++b->created;
+    }
+    if (r.kind == KORE_REQ_EIGEN) {
+        if (!r.evals || !r.nconv || r.max_pairs <= 0) return KORE_EINVAL;
+        // the batched engine on this plan's slots (one slot for an unshared pencil)
+        const int nslot = shared_eigen(r) ? kServeSlots : 1;
+        if (c->slots != nslot || c->slot_prec != r.precision) {
+            c->slots = 0;
+            c->factored = false;
+            for (bool &v : c->slot_valid) v = false;
+            KORE_TRY(kore_factor_reserve(c->plan, nslot, r.precision));
+            c->slots = nslot;
+            c->slot_prec = r.precision;
+        }
+        ServeSource src;
+        src.b = b; src.c = c; src.first = q;
+        q->status = KORE_EPENDING;
+        const int rc = kore_eigs_engine(c->plan, &src, c->slot_valid, kServeMaxNcv);
+        if (rc != KORE_OK) {
+            c->slots = 0;
+            for (bool &v : c->slot_valid) v = false;
+            return rc;
+        }
+        // the slots keep their factors: a later request at one of their shifts reuses them
+        return q->status;
+    }
+    if (c->slots != 0) {   // the plan held eigen slots: back to one shift
+        c->slots = 0;
+        c->slot_prec = -1;
+        for (bool &v : c->slot_valid) v = false;
     }
     if (!(c->factored && c->prec == r.precision && c->sre == r.sigma_re && c->sim == r.sigma_im)) {
         c->factored = false;
@@ -169,13 +294,6 @@ int run_request(kore_batch *b, Request *q, CachedPlan *c) {
         c->prec = r.precision;
         c->sre = r.sigma_re;
         c->sim = r.sigma_im;
-    }
-    if (r.kind == KORE_REQ_EIGEN) {
-        if (!r.evals || !r.nconv || r.max_pairs <= 0) return KORE_EINVAL;
-        kore_eps_opts o = r.opts;
-        o.target_re = r.sigma_re;
-        o.target_im = r.sigma_im;
-        return kore_eigs(c->plan, &o, r.evals, r.evecs, r.max_pairs, r.nconv, nullptr);
     }
     if (r.kind != KORE_REQ_FORCED || !r.rhs || !r.x) return KORE_EINVAL;
     const int64_t n = r.pencil->n;
@@ -204,7 +322,13 @@ void worker(kore_batch *b) {
                 b->cv_work.wait_for(lk, std::chrono::milliseconds(20));
             }
             q->t_start = Clock::now();
-            if (c) ++b->running;
+            if (c) {
+                ++b->running;
+                if (shared_eigen(q->r)) {
+                    c->engine = true;
+                    c->engine_prec = q->r.precision;
+                }
+            }
         }
         int st = q->status;
         if (c) st = run_request(b, q, c);
@@ -216,6 +340,7 @@ void worker(kore_batch *b) {
             if (c) {
                 --b->running;
                 c->busy = false;
+                c->engine = false;
                 c->last_use = ++b->clock;
                 int64_t actual = 0;
                 if (c->plan && kore_plan_bytes(c->plan, &actual) == KORE_OK && actual > c->bytes) {
@@ -311,6 +436,7 @@ int kore_batch_stats(kore_batch *b, int64_t *out) {
     out[5] = b->hits;
     out[6] = b->created;
     out[7] = b->evicted;
+    out[8] = b->joined;
     return KORE_OK;
 }
 

@@ -4,8 +4,11 @@
 kore runs one ``bin/solve.py`` process per problem.  Here a :class:`Server` keeps a
 queue of requests, each doing what one such run does (an eigensolve at a target,
 ``bin/solve.py:91-158``, or a forced solve at a shift, ``bin/solve.py:207-268``), runs
-several at once on plans of their own, admits them by the device memory their plans
-need and keeps uploaded, factorised plans for later requests on the same pencil.
+several at once, admits them by the device memory their plans need and keeps uploaded,
+factorised plans for later requests on the same pencil.  Eigen requests of one pencil
+are batched continuously: they run in the factor slots of one plan (the batched engine
+of ``kore_eigs_shifts``), sharing every launch, and a request that arrives while others
+of its pencil are on the GPU takes the next free slot.
 
     srv = Server(workers=4)
     P = PencilData(A, B, layout)                    # host arrays, no device memory yet
@@ -135,10 +138,10 @@ class Server:
         return out
 
     def stats(self):
-        a = np.zeros(8, dtype=np.int64)
+        a = np.zeros(9, dtype=np.int64)
         L.check(self.lib.kore_batch_stats(self._b, a.ctypes.data), "kore_batch_stats")
         names = ("submitted", "finished", "running", "queued", "device_bytes", "factor_cache_hits",
-                 "plans_created", "plans_evicted")
+                 "plans_created", "plans_evicted", "joined_running_engine")
         return dict(zip(names, (int(v) for v in a)))
 
     def close(self):

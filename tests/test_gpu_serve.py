@@ -91,3 +91,26 @@ def test_admission_under_a_small_budget(gpu_lib, case):
     assert st["finished"] == len(ts)
     assert st["plans_evicted"] >= 1
     assert st["device_bytes"] <= int(need * 1.2)
+
+
+def test_eigen_requests_join_a_running_engine(gpu_lib, case):
+    """Six eigen requests of one pencil: the first starts the batched engine on the
+    pencil's plan, the others are admitted into its slots (four) as they free up and
+    share its launches; each result equals the same request served alone."""
+    from kore_gb300.serve import Server
+    meta, A, B, P = data_of(case, "shell_m2_ek1e-4")
+    targets = [0.4j, 0.7j, 1.0j, 1.3j, 0.55j, 0.85j]
+    with Server(workers=1) as srv:
+        ts = [srv.submit_eigen(P, t, 6, seed=k + 1, vectors=True) for k, t in enumerate(targets)]
+        together = [srv.result(t) for t in ts]
+        st = srv.stats()
+    assert st["joined_running_engine"] >= len(targets) - 1, st
+    assert st["plans_created"] == 1
+    for k, (t, r) in enumerate(zip(targets, together)):
+        with Server(workers=1) as srv:
+            alone = srv.result(srv.submit_eigen(P, t, 6, seed=k + 1, vectors=True))
+        assert r["status"] == 0 and alone["nconv"] == r["nconv"] >= 6
+        assert np.array_equal(alone["evals"], r["evals"])
+        assert np.array_equal(alone["evecs"], r["evecs"])
+        ref, _ = shift_invert_eigs(A, B, t, 6, "TM")
+        assert match_eigs(r["evals"][:6], ref).max() < 1e-10
