@@ -311,6 +311,20 @@ int kore_tc_selftest(int device, int S, int nmat, double *max_rel_err);
  */
 int kore_gegenbauer_mult(int device, int N, const double *a0, double lam, int h, double *band);
 
+/*
+ * Flow diagnostics of velocity eigenvectors in a spherical shell (ricb in (0, 1),
+ * rcmb = 1), computed on `device`: for nvec vectors x, each npol poloidal blocks (degrees
+ * lpol) followed by ntor toroidal blocks (degrees ltor) of N complex Chebyshev
+ * coefficients (the velocity part of a solution in bin/assemble.py's order), out
+ * receives per vector and block the radial integrals of the kinetic energy, of
+ * integral(u . lap u) and of the internal dissipation (3 doubles, blocks in the order
+ * given).  Replaces flow_worker of bin/utils4pp.py:426-488, which bin/spin_doctor.py
+ * runs over the degrees in a process pool; the sums over degrees, the scaling by
+ * OmgTau Ek and the power-balance residuals are kore_gb300.diagnostics'.
+ */
+int kore_flow_diagnostics(int device, int N, double ricb, int npol, const int32_t *lpol, int ntor,
+                          const int32_t *ltor, const double *x, int nvec, double *out);
+
 /* Number of kernels this library launched since load (for launch accounting). */
 int64_t kore_kernel_launches(void);
 

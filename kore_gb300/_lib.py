@@ -26,7 +26,7 @@ WHICH = {"LM": 0, "SM": 1, "LR": 2, "SR": 3, "LI": 4, "SI": 5, "TM": 6, "TR": 7,
 EXPORTS = ("kore_plan_create", "kore_factor", "kore_factor_shifts", "kore_solve", "kore_solve_dev",
            "kore_solve_dev_noalloc", "kore_eigs", "kore_eigs_shifts", "kore_residual", "kore_plan_stream", "kore_profile",
            "kore_plan_bytes", "kore_plan_estimate_bytes", "kore_batch_create", "kore_batch_submit",
-           "kore_batch_poll", "kore_batch_stats", "kore_batch_destroy", "kore_tc_selftest", "kore_gegenbauer_mult", "kore_kernel_launches",
+           "kore_batch_poll", "kore_batch_stats", "kore_batch_destroy", "kore_tc_selftest", "kore_gegenbauer_mult", "kore_flow_diagnostics", "kore_kernel_launches",
            "kore_status_string", "kore_plan_destroy")
 
 
@@ -141,6 +141,7 @@ def _bind(lib):
     lib.kore_batch_destroy.argtypes = [P]
     lib.kore_tc_selftest.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
     lib.kore_gegenbauer_mult.argtypes = [C.c_int, C.c_int, P, C.c_double, C.c_int, P]
+    lib.kore_flow_diagnostics.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, P, C.c_int, P, P, C.c_int, P]
     for name in EXPORTS:
         if name not in ("kore_kernel_launches", "kore_status_string"):
             getattr(lib, name).restype = C.c_int

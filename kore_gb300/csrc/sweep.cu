@@ -23,7 +23,9 @@
 #include "kore_internal.cuh"
 #include "kore_tma.cuh"
 #include <cstddef>
+#include <map>
 #include <mutex>
+#include <tuple>
 
 namespace {
 
@@ -110,10 +112,12 @@ __device__ __forceinline__ void wait_count(const int *c, int target, int *err) {
 // dozen entries per row) with plain coalesced loads instead.
 constexpr int kTmaConsumerWarps = 4;
 constexpr int kTmaConsumers = 32 * kTmaConsumerWarps;
-// CTAs per SM: three CTAs of three or four 16 KB slots keep ~200 KB per SM in flight,
+// CTAs per SM: with three CTAs of three or four 16 KB slots, ~200 KB per SM is in flight
 // and a CTA's per-tile work (input vectors, reduction, signalling) overlaps the other
-// CTAs' streaming
+// CTAs' streaming.  Variants with 2 and 4 CTAs per SM are compiled too (deeper rings per
+// CTA, or more CTAs to overlap); the autotuner below picks one per plan shape.
 constexpr int kTmaCtasPerSm = 3;
+constexpr int kTmaVariants[] = {2, 3, 4};
 constexpr int kTmaThreads = kTmaConsumers + 64;   // + one producer warp + one dependency-checker warp
 constexpr int kChunkBytes = 16384;
 constexpr int kTileRows = 32;
@@ -206,8 +210,8 @@ __device__ __forceinline__ void decode_tile(int64_t g, int &k, const int64_t *st
     }
 }
 
-template <typename C>
-__global__ void __launch_bounds__(kTmaThreads, kTmaCtasPerSm) k_sweep_tma(const __grid_constant__ SweepTmaParams P) {
+template <typename C, int CPS>
+__global__ void __launch_bounds__(kTmaThreads, CPS) k_sweep_tma(const __grid_constant__ SweepTmaParams P) {
     using Shape = TmaShape<C>;
     constexpr int kCols = Shape::kCols, kCpw = Shape::kColsPerWarp;
     const SweepArgs &a = P.a;
@@ -736,10 +740,10 @@ SweepArgs sweep_args(const kore_plan *p, int nshift) {
     return a;
 }
 
-// Tensor maps, ring depth and the cooperative launch of k_sweep_tma; the completion
-// counters a.cnt are zeroed first.
+// Tensor maps, ring depth and the cooperative launch of k_sweep_tma with cps CTAs per SM
+// (2, 3 or 4); the completion counters a.cnt are zeroed first.
 template <typename C>
-int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st) {
+int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st, int cps = kTmaCtasPerSm) {
     SweepTmaParams P;
     P.a = a;
     const int rb = (int)sizeof(C) / 2;
@@ -750,15 +754,16 @@ int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st) {
     KORE_TRY(kore_encode_block_map(&P.maps[kMapH], p->d_Hm, rb, p->S, p->K, ns, p->f_stride(), kTileRows, kCols));
     KORE_TRY(kore_encode_block_map(&P.maps[kMapLU], p->d_LU, rb, p->S, p->lu_mats, ns, p->lu_stride(), kTileRows,
                                    kCols));
-    // ring depth: as many slots as fit kTmaCtasPerSm CTAs in the SM's shared memory
+    // ring depth: as many slots as fit cps CTAs in the SM's shared memory
     int smem_sm = 0, smem_blk = 0;
     KORE_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, p->device));
     KORE_CUDA_TRY(cudaDeviceGetAttribute(&smem_blk, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
-    auto kern = k_sweep_tma<C>;
+    void (*kern)(const SweepTmaParams) = (cps == 2) ? k_sweep_tma<C, 2> : (cps == 4) ? k_sweep_tma<C, 4>
+                                                                                    : k_sweep_tma<C, 3>;
     cudaFuncAttributes fa;
     KORE_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
     const size_t static_smem = fa.sharedSizeBytes + 1024;   // + the per-CTA reserve of the SM
-    const size_t budget = std::min<size_t>((size_t)smem_sm / kTmaCtasPerSm - static_smem,
+    const size_t budget = std::min<size_t>((size_t)smem_sm / cps - static_smem,
                                            (size_t)smem_blk - fa.sharedSizeBytes);
     int nst = kMaxRing;
     while (nst > 2 && tma_smem<C>(p->S, nst) > budget) --nst;
@@ -769,13 +774,55 @@ int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st) {
     int occ = 0;
     KORE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTmaThreads, smem));
     if (occ < 1) return KORE_EINVAL;
-    occ = std::min(occ, kTmaCtasPerSm);
+    occ = std::min(occ, cps);
     KORE_CUDA_TRY(cudaMemsetAsync(a.cnt, 0, (size_t)ns * p->sweep_stages() * p->K * sizeof(int), st));
     void *args[] = {&P};
     dim3 grid(p->num_sms * occ), block(kTmaThreads);
     KORE_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)kern, grid, block, args, smem, st));
     KORE_LAUNCHED(1);
     return KORE_OK;
+}
+
+// Autotuner of the sweep's CTAs per SM, keyed on the plan's shape: the first
+// non-accumulating sweep of a shape (padded block size, blocks, width of the level-0
+// coupling rows, precision, shifts) times every variant on its own work (a
+// non-accumulating sweep gives the same result each time it runs) and keeps the fastest
+// for every later sweep of that shape in the process.
+struct TuneKey {
+    int S, K, ell_w, prec, nshift;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(S, K, ell_w, prec, nshift) < std::tie(o.S, o.K, o.ell_w, o.prec, o.nshift);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune;
+
+template <typename C>
+int tune_sweep(kore_plan *p, const SweepArgs &a, int *best) {
+    cudaEvent_t e0, e1;
+    KORE_CUDA_TRY(cudaEventCreate(&e0));
+    KORE_CUDA_TRY(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    int rc = KORE_OK;
+    *best = kTmaCtasPerSm;
+    for (int cps : kTmaVariants) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 2 && rc == KORE_OK; ++rep) {   // the second run is timed
+            if (cudaEventRecord(e0, p->stream) != cudaSuccess) rc = KORE_ECUDA;
+            if (rc == KORE_OK) rc = launch_sweep<C>(p, a, p->stream, cps);
+            if (rc == KORE_OK && cudaEventRecord(e1, p->stream) != cudaSuccess) rc = KORE_ECUDA;
+            if (rc == KORE_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = KORE_ECUDA;
+            if (rc == KORE_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = KORE_ECUDA;
+        }
+        if (rc == KORE_EINVAL) { rc = KORE_OK; continue; }   // the variant does not fit this shape
+        if (rc != KORE_OK) break;
+        if (ms < best_ms) { best_ms = ms; *best = cps; }
+    }
+    // the chosen variant runs last, so the sweep's outputs are its own
+    if (rc == KORE_OK) rc = launch_sweep<C>(p, a, p->stream, *best);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
 }
 
 int sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int accumulate, const int *skip,
@@ -788,8 +835,26 @@ int sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int a
     a.out = x; a.accumulate = accumulate; a.cnt = p->d_cnt; a.err = p->d_err;
     a.skip = skip; a.skip_stride = (int)(sizeof(IrState) / sizeof(int));
     a.count = &p->d_ir->sweeps; a.count_total = &p->d_ir->sweeps_total;
-    const int s = (p->prec == KORE_PREC_FP64) ? launch_sweep<double2>(p, a, p->stream)
-                                              : launch_sweep<float2>(p, a, p->stream);
+    const bool fp64 = p->prec == KORE_PREC_FP64;
+    const TuneKey key{p->S, p->K, p->ell_w, p->prec, p->nshift};
+    int cps = 0;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) cps = it->second;
+    }
+    int s;
+    if (cps == 0 && !accumulate) {
+        s = fp64 ? tune_sweep<double2>(p, a, &cps) : tune_sweep<float2>(p, a, &cps);
+        if (s == KORE_OK) {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            g_tune[key] = cps;
+        }
+    } else {
+        if (cps == 0) cps = kTmaCtasPerSm;
+        s = fp64 ? launch_sweep<double2>(p, a, p->stream, cps) : launch_sweep<float2>(p, a, p->stream, cps);
+    }
+    p->sweep_cps = cps;
     if (p->prof) KORE_TRY(kore_prof_mark(p, 0, false));
     return s;
 }
@@ -1109,7 +1174,7 @@ int noalloc_sweep(kore_plan *p, NoAllocScratch *s, const double2 *b, const doubl
     a.f = s->f; a.z = s->z; a.x = s->x;
     a.out = x; a.accumulate = accumulate; a.cnt = s->cnt; a.err = &s->err;
     a.skip = skip; a.skip_stride = 0; a.count = &s->ir.sweeps; a.count_total = &s->ir.sweeps_total;
-    return launch_sweep<C>(p, a, st);
+    return launch_sweep<C>(p, a, st, p->sweep_cps > 0 ? p->sweep_cps : kTmaCtasPerSm);
 }
 
 int noalloc_solve(kore_plan *p, NoAllocScratch *s, const double2 *b_dev, double2 *x_dev, double tol, cudaStream_t st) {
