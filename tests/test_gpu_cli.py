@@ -20,7 +20,8 @@ def write_case(tmp, meta, A, B):
     os.makedirs(os.path.join(tmp, "bin"), exist_ok=True)
     tau = complex(*meta["tau"])
     lines = [f"{k} = {meta[k]!r}" for k in ("hydro", "magnetic", "thermal", "compositional", "m", "symm", "ricb",
-                                            "N", "lmax", "forcing", "nev", "tol", "maxit", "which_eigenpairs", "B0")]
+                                            "N", "lmax", "forcing", "nev", "tol", "maxit", "which_eigenpairs", "B0",
+                                            "Ek")]
     lines.append(f"tau = complex({tau.real!r}, {tau.imag!r})")
     lines.append("B0_l = 1")
     with open(os.path.join(tmp, "bin", "parameters.py"), "w") as f:
@@ -85,3 +86,30 @@ def test_cli_binary_output_matches_text(gpu_lib, case, tmp_path):
     for part in ("real", "imag"):
         txt = np.loadtxt(tmp_path / f"{part}_flow.field")
         np.testing.assert_allclose(np.load(tmp_path / f"{part}_flow.field.npy"), txt, rtol=1e-17, atol=0)
+
+
+def test_cli_spin_doctor(gpu_lib, case, tmp_path):
+    """solve.py then spin_doctor.py in a case directory (the reference's post-processing
+    order): the printed table and flow.dat hold the power balance of every solution,
+    equal to the oracle's diagnostics of the written fields."""
+    from kore_gb300.structure import ell
+    from oracle.diag_ref import flow_diagnostics
+    meta, A, B = case("shell_m1_ek1e-4")
+    write_case(str(tmp_path), meta, A, B)
+    run_cli(str(tmp_path), "-st_type", "sinvert", "-kore_precision", "mixed")
+    cmd = [sys.executable, os.path.join(ROOT, "kore_gb300", "cli", "spin_doctor.py")]
+    r = subprocess.run(cmd, cwd=str(tmp_path), capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    dat = np.loadtxt(tmp_path / "eigenvalues0.dat").reshape(-1, 2)
+    flow = np.loadtxt(tmp_path / "flow.dat").reshape(-1, 14)
+    assert flow.shape[0] == dat.shape[0]
+    n = meta["sizmat"] // 2
+    X = np.loadtxt(tmp_path / "real_flow.field") + 1j * np.loadtxt(tmp_path / "imag_flow.field")
+    lp, lt = ell(meta["m"], meta["lmax"], meta["symm"])
+    for k in range(dat.shape[0]):
+        ref = flow_diagnostics(X[:, k], lp, lt, meta["N"], meta["ricb"], dat[k, 0] + 1j * dat[k, 1], Ek=meta["Ek"])
+        got = dict(zip(("KE", "KP", "KT", "Dkin", "Dint"), flow[k, :5]))
+        for key, v in got.items():
+            assert abs(v - ref[key]) <= 1e-9 * abs(ref[key]), (k, key)
+        assert abs(flow[k, 9] - ref["resid1"]) <= 1e-5 * max(ref["resid1"], 1e-12)
+        assert flow[k, 9] < 1e-4

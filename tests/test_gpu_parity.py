@@ -138,12 +138,18 @@ def test_eigs_convective_onset(gpu_lib, case, name, omega_c):
     assert abs(lam[i].real) < 1e-5 and abs(lam[i].imag - omega_c) < 1e-6
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-10)])
 @pytest.mark.parametrize("name", ["mac_dipole_small", "mac_quadrupole_small", "shell_m2_small"])
-def test_eigs_other_pencils(gpu_lib, case, name):
+def test_eigs_other_pencils(gpu_lib, case, name, precision, tol):
+    """Magneto-Archimedes-Coriolis pencils (dipole: superblocks {upol, btor, theta} /
+    {utor, bpol}; quadrupole: degree pairs merged for the l +- 2 coupling) and an m=2
+    shell, at the bars of the eigenvalue comparison: FP64 1e-12, mixed 1e-10."""
     meta, A, B = case(name)
     tau = complex(*meta["tau"])
     ref, _ = shift_invert_eigs(A, B, tau, meta["nev"], "TM")
     with make_pencil(meta, A, B) as p:
-        E = run_eps(p, meta, "fp64", which="TM")
-    err = match_eigs(E.eigenvalues()[:meta["nev"]], ref)
-    assert err.max() < 1e-10, err
+        E = run_eps(p, meta, precision, which="TM")
+    lam, X = E.eigenvalues(), E.eigenvectors()
+    err = match_eigs(lam[:meta["nev"]], ref)
+    assert err.max() < tol, err
+    assert eig_residuals(A, B, lam[:meta["nev"]], X[:, :meta["nev"]]).max() < 1e-12
