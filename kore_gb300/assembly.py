@@ -42,18 +42,59 @@ def ncheb(Ek):
     return max(48, out + out % 2)
 
 
-def chebco(powr, N, tol, ricb, rcmb=RCMB):
-    """First N Chebyshev coefficients of r^powr on [ricb, rcmb] (``bin/utils.py:251-269``)."""
+def gauss_radii(N, ricb, rcmb=RCMB):
+    """The radii of the N Chebyshev-Gauss points x_i = cos(pi (i + 1/2) / N)."""
     i = np.arange(N)
     xi = np.cos(np.pi * (i + 0.5) / N)
     if ricb == 0:
-        ai = (rcmb * xi) ** powr
-    else:
-        ai = (ricb + (rcmb - ricb) * (xi + 1) / 2.0) ** powr
-    out = sfft.dct(ai, type=2) / N
+        return rcmb * xi
+    return ricb + (rcmb - ricb) * (xi + 1) / 2.0
+
+
+def chebco_values(fi, tol):
+    """Chebyshev coefficients of the function whose values at the Chebyshev-Gauss points
+    are fi (DCT-II), entries of magnitude <= tol set to zero (``bin/utils.py:200-222``)."""
+    N = fi.size
+    out = sfft.dct(fi, type=2) / N
     out[0] = out[0] / 2.0
     out[np.abs(out) <= tol] = 0.0
     return out
+
+
+def chebco(powr, N, tol, ricb, rcmb=RCMB):
+    """First N Chebyshev coefficients of r^powr on [ricb, rcmb] (``bin/utils.py:251-269``)."""
+    return chebco_values(gauss_radii(N, ricb, rcmb) ** powr, tol)
+
+
+# Poloidal scalar of the dipole background field outside a point dipole, h(r) = r^-2 / 2,
+# and its r-derivatives: h^(j)(r) = c_j r^e_j (``bin/utils.py:555-760``, kind 'dipole').
+_DIPOLE_H = ((0.5, -2), (-1.0, -3), (3.0, -4), (-12.0, -5))
+
+
+def dipole_h(r, j, rpow=0):
+    """r^rpow times the j-th r-derivative of the dipole's poloidal scalar."""
+    c, e = _DIPOLE_H[j]
+    return c * r ** (e + rpow)
+
+
+def dipole_norm(ricb, cnorm="mag_energy"):
+    """Amplitude of the dipole background field (``bin/utils.py:837-890``): unit total
+    magnetic energy in the shell ('mag_energy', twice that for 'Schmitt2012', by a
+    240-point Chebyshev-Gauss quadrature), unit rms radial field at the outer boundary
+    ('rms_cmb'), or a number given as is."""
+    l, L = 1, 2
+    if cnorm == "rms_cmb":
+        return float(np.sqrt(2 * l + 1) / (L * dipole_h(np.array([1.0]), 0)[0]))
+    if cnorm in ("mag_energy", "Schmitt2012"):
+        N = 240
+        xk = np.cos((np.arange(N) + 0.5) * np.pi / N)
+        sqx = np.sqrt(1 - xk ** 2)
+        rk = 0.5 * (1 - ricb) * (xk + 1) + ricb
+        y0, y1 = dipole_h(rk, 0), dipole_h(rk, 1)
+        f0 = 4 * np.pi * L / (2 * l + 1)
+        integ = (np.pi / N) * ((1 - ricb) / 2) * np.sum(sqx * f0 * ((L + 1) * y0 ** 2 + 2 * rk * y0 * y1 + rk ** 2 * y1 ** 2))
+        return float((1.0 if cnorm == "mag_energy" else 2.0) / np.sqrt(integ))
+    return float(cnorm)
 
 
 def conv_mat(lam, N):
@@ -181,13 +222,18 @@ def mult_mat_gpu(a0, lam, device=0):
 
 
 class RadialOperators:
-    """The r^X D^Y operators of the two hydrodynamic sections for one (N, ricb).
-    ``device``: compute the multiplication operators on that GPU (``mult_mat_gpu``)."""
+    """The radial operators ``r^X D^Y`` (and, with a background field of amplitude
+    ``field``, ``r^X h^(J) D^Y``) of the equations' sections for one (N, ricb).
+    Section 'u' (the double-curl momentum equation) leaves 4 rows for boundary
+    conditions, every other section 2.  ``device``: compute the multiplication operators
+    on that GPU (``mult_mat_gpu``)."""
 
-    def __init__(self, N, ricb, tol=1e-9, device=None):
+    def __init__(self, N, ricb, tol=1e-9, device=None, field=None):
         self.N = N
         self.ricb = ricb
+        self.tol = tol
         self.device = device
+        self.field = field
         rp = [chebco(x, N, tol, ricb) for x in range(7)]
         S = [conv_mat(l, N) for l in range(4)]
         D = [None] + [diff_mat(l, N, ricb) for l in range(1, 5)]
@@ -198,13 +244,25 @@ class RadialOperators:
         self._rp, self._Sto, self._D, self._G = rp, Sto, D, {4: G4, 2: G2}
         self._cache = {}
 
-    def op(self, rx, dx, section):
-        """Operator ``r<rx>_D<dx>_<section>`` with the tau rows emptied."""
-        key = (rx, dx, section)
+    def field_coeffs(self, rx, j):
+        """Chebyshev coefficients of field * r^rx h^(j)(r); as the reference, small
+        coefficients are dropped before the amplitude is applied (``bin/utils.py:800-834``,
+        ``bin/submatrices.py:121-128``)."""
+        key = ("h", rx, j)
+        if key not in self._cache:
+            fi = dipole_h(gauss_radii(self.N, self.ricb), j, rx)
+            self._cache[key] = self.field * chebco_values(fi, self.tol)
+        return self._cache[key]
+
+    def op(self, rx, dx, section, h=None):
+        """Operator ``r<rx>_D<dx>_<section>`` (``r<rx>_h<h>_D<dx>_<section>`` with h) with
+        the boundary rows emptied."""
+        key = (rx, dx, section, h)
         if key in self._cache:
             return self._cache[key]
         g = 4 if section == "u" else 2
-        a = self._Sto[dx] @ self._rp[rx]
+        c0 = self._rp[rx] if h is None else self.field_coeffs(rx, h)
+        a = self._Sto[dx] @ c0
         Mm = mult_mat(a, dx) if self.device is None else mult_mat_gpu(a, dx, self.device)
         M = self._G[g][g - dx] @ Mm
         if dx > 0:
@@ -228,6 +286,111 @@ def boundary_values(x, N, nder, ricb, rcmb=RCMB):
     return out
 
 
+def kron_sum(lrow, lcol, terms):
+    """Sum over terms (d, coef, M) of kron(P, M), where P[k, j] = coef(l_k) for the blocks
+    k of degree l_k = lrow[k] and j of degree lcol[j] = l_k + d: the coupling of degree l
+    to degree l + d in the l-block layout of two sections.  ``coef`` takes an array of
+    degrees.  None if no block couples."""
+    lrow = np.asarray(lrow)
+    lcol = np.asarray(lcol)
+    pos = {int(l): j for j, l in enumerate(lcol)}
+    out = None
+    for d, coef, M in terms:
+        ks = np.array([k for k, l in enumerate(lrow) if int(l) + d in pos], dtype=np.int64)
+        if ks.size == 0:
+            continue
+        js = np.array([pos[int(lrow[k]) + d] for k in ks], dtype=np.int64)
+        vals = np.asarray(coef(lrow[ks].astype(float)), dtype=complex) * np.ones(ks.size)
+        P = ss.csr_matrix((vals, (ks, js)), shape=(lrow.size, lcol.size))
+        t = ss.kron(P, M, format="csr")
+        out = t if out is None else out + t
+    return out
+
+
+def momentum_blocks(op, m, lp, lt, visc, wf, Gaspard=1.0, pu=0, pv=0):
+    """Blocks of the momentum equation (``bin/operators.py:22-124,136-195``, non-anelastic):
+    section u (r.curl curl, poloidal degrees lp) and section v (r.curl, toroidal degrees
+    lt).  Returns (App, Apt, Atp, Att, Up, Ut): the time derivative i w u plus Coriolis
+    minus viscous terms on the diagonal, the Coriolis coupling l -> l +- 1 between the
+    sections, and the time-derivative operators Up, Ut of B.  The reference multiplies
+    the equations by r^2 (section u) and r^3 (section v) more for the dipole field: pu,
+    pv raise the powers of r accordingly."""
+    m = float(m)
+    u = lambda rx, dx: op(rx + pu, dx, "u")
+    v = lambda rx, dx: op(rx + pv, dx, "v")
+    L = lambda l: l * (l + 1)
+    # section u, degree l: u = L (L r2 - 2 r3 D - r4 D2), Coriolis 2im (-L r2 + 2 r3 D + r4 D2),
+    # viscous L (-L (l+2)(l-1) r0 + 2L r2 D2 - 4 r3 D3 - r4 D4)
+    Up = kron_sum(lp, lp, [(0, lambda l: L(l) * L(l), u(2, 0)), (0, lambda l: -2 * L(l), u(3, 1)),
+                           (0, lambda l: -L(l), u(4, 2))])
+    Cp = kron_sum(lp, lp, [(0, lambda l: -L(l) * 2 * m, u(2, 0)), (0, lambda l: 4 * m + 0 * l, u(3, 1)),
+                           (0, lambda l: 2 * m + 0 * l, u(4, 2))])
+    Vp = kron_sum(lp, lp, [(0, lambda l: -L(l) * L(l) * (l + 2) * (l - 1), u(0, 0)),
+                           (0, lambda l: 2 * L(l) * L(l), u(2, 2)), (0, lambda l: -4 * L(l), u(3, 3)),
+                           (0, lambda l: -L(l), u(4, 4))])
+    Ut = kron_sum(lt, lt, [(0, L, v(2, 0))])
+    Ct = kron_sum(lt, lt, [(0, lambda l: -2 * m + 0 * l, v(2, 0))])
+    Vt = kron_sum(lt, lt, [(0, lambda l: -L(l) * L(l), v(0, 0)), (0, lambda l: 2 * L(l), v(1, 1)),
+                           (0, L, v(2, 2))])
+    App = (1j * wf) * Up + (1j * Gaspard) * Cp - visc * Vp
+    Att = (1j * wf) * Ut + (1j * Gaspard) * Ct - visc * Vt
+    # Coriolis coupling: to degree l-1 with C- = (l^2-1) sqrt(l^2-m^2) / (2l-1),
+    # 2C- ((l-1) r^a - r^b D); to l+1 with C+ = l (l+2) sqrt((l+m+1)(l-m+1)) / (2l+3),
+    # 2C+ (-(l+2) r^a - r^b D); (a, b) = (3, 4) in section u and (1, 2) in section v
+    cm = lambda l: (l ** 2 - 1) * np.sqrt(l ** 2 - m ** 2) / (2 * l - 1.0)
+    cp = lambda l: l * (l + 2.0) * np.sqrt((l + m + 1.0) * (l - m + 1)) / (2.0 * l + 3.0)
+
+    def coriolis(lrow, lcol, w, a, b):
+        return Gaspard * kron_sum(lrow, lcol, [
+            (-1, lambda l: 2 * cm(l) * (l - 1), w(a, 0)), (-1, lambda l: -2 * cm(l), w(b, 1)),
+            (1, lambda l: 2 * cp(l) * -(l + 2), w(a, 0)), (1, lambda l: -2 * cp(l), w(b, 1))])
+
+    Apt = coriolis(lp, lt, u, 3, 4)
+    Atp = coriolis(lt, lp, v, 1, 2)
+    return App, Apt, Atp, Att, Up, Ut
+
+
+def bc_block(rows_list, nrow, N1):
+    """Block-diagonal matrix holding, for each l-block k, the boundary rows rows_list[k]
+    (nrow rows of N1 Chebyshev coefficients) in its first nrow rows."""
+    data, ri, ci = [], [], []
+    for k, rows in enumerate(rows_list):
+        for q in range(nrow):
+            nz = np.nonzero(rows[q])[0]
+            data.append(rows[q][nz])
+            ri.append(np.full(nz.size, k * N1 + q))
+            ci.append(k * N1 + nz)
+    n = len(rows_list) * N1
+    return ss.csr_matrix((np.concatenate(data).astype(complex), (np.concatenate(ri), np.concatenate(ci))),
+                         shape=(n, n))
+
+
+def velocity_bc_blocks(lp, lt, N, ricb, bci=1, bco=1, forcing=0):
+    """Boundary rows of the velocity (``bc_u_spherical``, ``bin/assemble.py:1188-1296``,
+    ricb > 0): in section u, u_r = 0 and no-slip (bc = 1) or stress-free (0) at the outer
+    then the inner boundary; in section v, no-slip or stress-free at both."""
+    N1 = N
+    Tb = boundary_values(1, N, 5, ricb)
+    Ta = boundary_values(-1, N, 4, ricb)
+
+    def rows_u(l):
+        L = l * (l + 1)
+        rows = np.zeros((4, N1), dtype=complex)
+        rows[0] = Tb[:, 0]
+        if bco == 0:
+            rows[1] = (Tb[:, 2] - (2 - L) * Tb[:, 0] / RCMB ** 2) if forcing == 9 else RCMB * Tb[:, 2]
+        else:
+            rows[1] = (Tb[:, 1] + Tb[:, 0]) if forcing == 9 else Tb[:, 1]
+        rows[2] = Ta[:, 0]
+        rows[3] = ricb * Ta[:, 2] if bci == 0 else Ta[:, 1]
+        return rows
+
+    rv = np.zeros((2, N1), dtype=complex)
+    rv[0] = (-RCMB * Tb[:, 1] + Tb[:, 0]) if bco == 0 else Tb[:, 0]
+    rv[1] = (-ricb * Ta[:, 1] + Ta[:, 0]) if bci == 0 else Ta[:, 0]
+    return bc_block([rows_u(float(l)) for l in lp], 4, N1), bc_block([rv for _ in lt], 2, N1)
+
+
 def hydro_pencil(m, symm, Ek, N, lmax, ricb=0.35, bci=1, bco=1, forcing=0, forcing_frequency=0.0,
                  forcing_amplitude_cmb=1.0, forcing_amplitude_icb=0.0, Gaspard=1.0, ViscosD=None,
                  with_norm=False, device=None):
@@ -245,122 +408,15 @@ def hydro_pencil(m, symm, Ek, N, lmax, ricb=0.35, bci=1, bco=1, forcing=0, forci
     if (lmax - m + 1) % 2:
         raise ValueError("lmax - m + 1 must be even")
     visc = Ek if ViscosD is None else ViscosD
-    N1 = radial_size(N, ricb)
-    nb = (lmax - m + 1) // 2
     lp, lt = ell(m, lmax, symm)
     wf = forcing_frequency if forcing else 0.0
     R = RadialOperators(N, ricb, device=device)
-    op = R.op
-    lp_f = lp.astype(float)
-    lt_f = lt.astype(float)
-    Lp = lp_f * (lp_f + 1)
-    Lt = lt_f * (lt_f + 1)
-
-    def kdiag(coef, M):
-        return ss.kron(ss.diags(coef), M, format="csr")
-
-    # --- diagonal blocks: poloidal (section u) and toroidal (section v)
-    uu = [(Lp * Lp, op(2, 0, "u")), (-2 * Lp, op(3, 1, "u")), (-Lp, op(4, 2, "u"))]            # u(l,'u')
-    cu = [(-Lp * 2 * m, op(2, 0, "u")), (2 * 2 * m * np.ones(nb), op(3, 1, "u")),
-          (2 * m * np.ones(nb), op(4, 2, "u"))]                                                # /(1j) coriolis
-    vu = [(-Lp * Lp * (lp_f + 2) * (lp_f - 1), op(0, 0, "u")), (2 * Lp * Lp, op(2, 2, "u")),
-          (-4 * Lp, op(3, 3, "u")), (-Lp, op(4, 4, "u"))]                                      # viscous
-    uv = [(Lt, op(2, 0, "v"))]
-    cv = [(-2 * m * np.ones(nb), op(2, 0, "v"))]
-    vv = [(-Lt * Lt, op(0, 0, "v")), (2 * Lt, op(1, 1, "v")), (Lt, op(2, 2, "v"))]
-
-    def sumk(terms, scale=1.0):
-        out = None
-        for c, M in terms:
-            t = kdiag(scale * c, M)
-            out = t if out is None else out + t
-        return out
-
-    u_p = sumk(uu)
-    u_t = sumk(uv)
-    App = (1j * wf) * u_p + (1j * Gaspard) * sumk(cu) - visc * sumk(vu)
-    Att = (1j * wf) * u_t + (1j * Gaspard) * sumk(cv) - visc * sumk(vv)
-
-    # --- Coriolis coupling l <-> l+-1 between the sections
-    def cpair(l, sgn):
-        if sgn < 0:
-            return (l ** 2 - 1) * np.sqrt(l ** 2 - m ** 2) / (2 * l - 1.0)
-        return l * (l + 2.0) * np.sqrt((l + m + 1.0) * (l - m + 1)) / (2.0 * l + 3.0)
-
-    def coupling(lrow, lcol, sec, terms):
-        rows, cols, c_by_term = [], [], [[] for _ in terms]
-        for k, l in enumerate(lrow):
-            for sgn in (-1, 1):
-                w = np.nonzero(lcol == l + sgn)[0]
-                if w.size == 0:
-                    continue
-                rows.append(k)
-                cols.append(int(w[0]))
-                C = cpair(float(l), sgn)
-                for ti, f in enumerate(terms):
-                    c_by_term[ti].append(2 * C * f(float(l), sgn))
-        out = None
-        for ti, (_, M) in enumerate(terms_ops(sec)):
-            P = ss.csr_matrix((np.array(c_by_term[ti]), (rows, cols)), shape=(len(lrow), len(lcol)))
-            t = ss.kron(P, M, format="csr")
-            out = t if out is None else out + t
-        return Gaspard * out
-
-    def terms_ops(sec):
-        if sec == "u":
-            return [(None, op(3, 0, "u")), (None, op(4, 1, "u"))]
-        return [(None, op(1, 0, "v")), (None, op(2, 1, "v"))]
-
-    # section u row l, utor column l-1: 2C((l-1) r3D0 - r4D1); l+1: 2C(-(l+2) r3D0 - r4D1)
-    fu = [lambda l, s: (l - 1) if s < 0 else -(l + 2), lambda l, s: -1.0]
-    Apt = coupling(lp, lt, "u", fu)
-    Atp = coupling(lt, lp, "v", fu)
-
-    # --- tau rows (bc_u_spherical, no-slip / stress-free, ricb > 0)
-    Tb = boundary_values(1, N, 5, ricb)
-    Ta = boundary_values(-1, N, 4, ricb)
-
-    def bc_rows_u(l):
-        L = l * (l + 1)
-        rows = np.zeros((4, N1), dtype=complex)
-        if bco == 0:
-            rows[0] = Tb[:, 0]
-            rows[1] = (Tb[:, 2] - (2 - L) * Tb[:, 0] / RCMB ** 2) if forcing == 9 else RCMB * Tb[:, 2]
-        else:
-            rows[0] = Tb[:, 0]
-            rows[1] = (Tb[:, 1] + Tb[:, 0]) if forcing == 9 else Tb[:, 1]
-        if bci == 0:
-            rows[2] = Ta[:, 0]
-            rows[3] = ricb * Ta[:, 2]
-        else:
-            rows[2] = Ta[:, 0]
-            rows[3] = Ta[:, 1]
-        return rows
-
-    def bc_rows_v():
-        rows = np.zeros((2, N1), dtype=complex)
-        rows[0] = (-RCMB * Tb[:, 1] + Tb[:, 0]) if bco == 0 else Tb[:, 0]
-        rows[1] = (-ricb * Ta[:, 1] + Ta[:, 0]) if bci == 0 else Ta[:, 0]
-        return rows
-
-    def bc_block(rows_list, nrow):
-        data, ri, ci = [], [], []
-        for k, rows in enumerate(rows_list):
-            for q in range(nrow):
-                nz = np.nonzero(rows[q])[0]
-                data.append(rows[q][nz])
-                ri.append(np.full(nz.size, k * N1 + q))
-                ci.append(k * N1 + nz)
-        return ss.csr_matrix((np.concatenate(data), (np.concatenate(ri), np.concatenate(ci))),
-                             shape=(len(rows_list) * N1, len(rows_list) * N1))
-
-    BCp = bc_block([bc_rows_u(float(l)) for l in lp], 4)
-    BCt = bc_block([bc_rows_v() for _ in lt], 2)
+    App, Apt, Atp, Att, u_p, u_t = momentum_blocks(R.op, m, lp, lt, visc, wf, Gaspard)
+    BCp, BCt = velocity_bc_blocks(lp, lt, N, ricb, bci, bco, forcing)
     A = ss.bmat([[App + BCp, Apt], [Atp, Att + BCt]], format="csr").astype(np.complex128)
     A.eliminate_zeros()
-    n = 2 * nb * N1
     if forcing == 0:
-        B = ss.bmat([[-u_p, None], [None, -u_t]], format="csr").astype(np.float64)
+        B = ss.bmat([[-u_p, None], [None, -u_t]], format="csr").real.astype(np.float64)
         B.eliminate_zeros()
         bnorm = ss.linalg.norm(B)
         if with_norm:

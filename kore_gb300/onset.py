@@ -67,8 +67,9 @@ class OnsetSearch:
     def sigma(self, log10_ra):
         return self.leading(10.0 ** log10_ra)[0]
 
-    def bracket(self, x1, x2=None, dx=0.01):
-        """A bracket [x1, x2] of the growth-rate root in log10(Ra) (find_Rac.py: bracket_brentq)."""
+    def bracket(self, x1, x2=None, dx=0.01, maxsteps=100):
+        """A bracket [x1, x2] of the growth-rate root in log10(Ra) (find_Rac.py: bracket_brentq).
+        The search gives up (RuntimeError) after ``maxsteps`` steps of dx without a sign change."""
         y1 = self.sigma(x1)
         dx = abs(dx)
         if x2 is not None:
@@ -80,18 +81,20 @@ class OnsetSearch:
         if x2 is None:
             step = -dx if y1 > 0 else dx
             x2 = x1
-            while True:
+            for _ in range(maxsteps):
                 x2 += step
                 y2 = self.sigma(x2)
                 if y1 * y2 < 0:
                     break
                 x1, y1 = x2, y2
+            else:
+                raise RuntimeError(f"no sign change of the growth rate within {maxsteps} steps of {dx} from {x1 - maxsteps * step:g}")
         return x1, x2
 
-    def critical(self, log10_ra0, dx=0.01, tol=1e-6, maxiter=200):
+    def critical(self, log10_ra0, dx=0.01, tol=1e-6, maxiter=200, maxsteps=100):
         """(Ra_c, omega_c): the Rayleigh number where the leading growth rate vanishes and the
         frequency of that mode (the imaginary part of its eigenvalue)."""
-        x1, x2 = self.bracket(log10_ra0, dx=dx)
+        x1, x2 = self.bracket(log10_ra0, dx=dx, maxsteps=maxsteps)
         lo, hi = min(x1, x2), max(x1, x2)
         xc = brentq(self.sigma, lo, hi, xtol=tol, rtol=tol, maxiter=maxiter)
         Ra_c = 10.0 ** xc

@@ -67,6 +67,16 @@ CASES = {
         "symm": "1", "Ek": "1e-3", "N": "24", "lmax": "16", "itau": "0.1",
         "magnetic": "1", "thermal": "1", "B0": "'dipole'", "Pm": "1e-3",
         "Lambda": "0.1", "Ra_gap": "1e5", "nev": "8"}, True),
+    # dipole MAC case of 3,200 unknowns, antisymmetric flow, fixed heat flux at the outer boundary
+    "mac_dipole_medium": ("bin/parameters.py", {
+        "symm": "-1", "Ek": "1e-4", "N": "40", "lmax": "32", "itau": "0.1",
+        "magnetic": "1", "thermal": "1", "B0": "'dipole'", "Pm": "1e-3",
+        "Lambda": "1e-4", "Ra_gap": "5e5", "bco_thermal": "1", "nev": "8"}, True),
+    # dipole MAC case with internal heating, m=2, fixed heat flux at the inner boundary
+    "mac_dipole_internal": ("bin/parameters.py", {
+        "m": "2", "symm": "1", "Ek": "1e-3", "N": "24", "lmax": "17", "itau": "0.1",
+        "magnetic": "1", "thermal": "1", "B0": "'dipole'", "heating": "'internal'",
+        "Pm": "1e-3", "Lambda": "0.1", "Ra_gap": "1e5", "bci_thermal": "1", "nev": "8"}, True),
     # small quadrupole-field case (l +- 2 coupling through B0)
     "mac_quadrupole_small": ("bin/parameters.py", {
         "symm": "1", "Ek": "1e-3", "N": "24", "lmax": "16", "itau": "0.1",
@@ -75,7 +85,8 @@ CASES = {
 }
 
 DERIVED = ("m symm ricb N lmax hydro magnetic thermal compositional B0 forcing "
-           "forcing_frequency nev tol maxit which_eigenpairs Ek").split()
+           "forcing_frequency nev tol maxit which_eigenpairs Ek Em Le2 Prandtl Ra heating "
+           "bci_thermal bco_thermal cnorm").split()
 
 
 def edit_params(text, overrides):

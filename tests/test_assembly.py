@@ -60,3 +60,36 @@ def test_forced_matrix_is_scaled_shift_of_eigen_pencil():
         M = nrm * (Ae - (1j * w) * Be)
         assert abs(Af - M).max() <= 1e-12 * abs(Af).max()
         assert abs(bf - forcing_vector(m, symm, N, lmax, ricb, 10, w)).max() == 0
+
+
+MAC = ["mac_dipole_small", "mac_dipole_medium", "mac_dipole_internal"]
+
+
+@pytest.mark.parametrize("name", MAC)
+def test_mac_dipole_matches_reference_assembly(case, name):
+    """The dipole MAC restatement (kore_gb300.assembly_mac) against the pencils the
+    reference's own compute_profiles.py/submatrices.py/assemble.py produced: both
+    symmetries, differential and internal heating, isothermal and fixed-flux thermal
+    boundaries."""
+    from kore_gb300.assembly_mac import mac_pencil
+    meta, A, B = case(name)
+    A2, B2 = mac_pencil(meta["m"], meta["symm"], meta["Ek"], meta["N"], meta["lmax"], meta["ricb"],
+                        Em=meta["Em"], Le2=meta["Le2"], Prandtl=meta["Prandtl"], Ra=meta["Ra"],
+                        heating=meta["heating"], bci_thermal=meta["bci_thermal"],
+                        bco_thermal=meta["bco_thermal"], cnorm=meta["cnorm"])
+    assert A2.shape == A.shape and B2.shape == B.shape
+    assert ssl.norm(A2 - A) <= 1e-14 * ssl.norm(A)
+    assert ssl.norm(B2 - B) <= 1e-14 * ssl.norm(B)
+    D = abs(A2 - A).tocsr()
+    rowmax = np.asarray(abs(A).max(axis=1).todense()).ravel()
+    assert (D.multiply(1.0 / np.maximum(rowmax, 1e-300)[:, None])).max() < 1e-13
+
+
+def test_mac_pencil_is_affine_in_rayleigh_number():
+    from kore_gb300.assembly_mac import mac_pencil, mac_pencil_parts
+    kw = dict(Em=0.1, Le2=1e-3, Prandtl=1.0)
+    A0, Ab, B, nrm = mac_pencil_parts(1, -1, 1e-3, 20, 12, 0.35, **kw)
+    for Ra in (0.0, 3.7e5):
+        A, B2 = mac_pencil(1, -1, 1e-3, 20, 12, 0.35, Ra=Ra, **kw)
+        assert ssl.norm(A - (A0 - Ra * 1e-6 * Ab) / nrm) <= 1e-15 * ssl.norm(A)
+        assert ssl.norm(B2 - B / nrm) == 0.0
