@@ -157,8 +157,9 @@ def rel_residuals(A, B, lam, X):
     return np.array(out)
 
 
-def time_arm(p, torch, stream, w, precision, steps, warmup, seed0=1):
-    m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[w]
+def time_arm(p, torch, stream, spec, precision, steps, warmup, seed0=1):
+    """Timed eigensolves of (tau, nev, which) = spec: CUDA events on the plan's stream."""
+    tau, nev, which = spec
     for s in range(warmup):
         run_eps(p, tau, nev, which, precision, seed0 + s)
     lat, pairs = [], 0
@@ -429,6 +430,92 @@ def forced_bench(args, local, c=None, emit=True):
 # serving ranges (lmax in [60, 600], N in [48, 400], Ek log-uniform in [1e-7, 1e-4],
 # m in 0..8); 70% eigen (nev 4..16, target i*U[-2, 2]) and 30% forced (forcing 10,
 # shift i*U[-2, 2]), at each arrival rate in `rates` (requests/s).
+# Config 3: the dipole MAC shell (Lorentz force, induction, buoyancy; insulating inner
+# core and mantle; differential heating) at twice the critical Rayleigh number of its
+# m mode.  The critical Rayleigh number comes from the onset search of
+# tests/jones2000/find_Rac.py (FP64, target 0, 'TR', 16 pairs) started at log10_ra0;
+# the timed solves are at the target tau.  symm = 1: equatorially symmetric flow, as in
+# the reference's onset tests.
+MAC = {
+    "mac3": dict(m=1, symm=1, Ek=1e-6, N=200, lmax=200, ricb=0.35, Em=1e-3, Le2=1e-8, Prandtl=1.0,
+                 tau=0.1j, nev=8, which="TM", log10_ra0=8.9),
+}
+
+
+def describe_mac(c):
+    return (f"dipole MAC shell ricb={c['ricb']} no-slip, insulating, m={c['m']} symm={c['symm']} Ek={c['Ek']:g} "
+            f"Em={c['Em']:g} Le2={c['Le2']:g} Pr={c['Prandtl']:g} N={c['N']} lmax={c['lmax']}, differential heating, "
+            f"Ra = 2 Ra_c, target {c['tau'].imag:g}i, nev={c['nev']}, which={c['which']}")
+
+
+def mac_bench(args, local, c=None, emit=True):
+    """Config 3: eigenpairs/s of the dipole MAC shell at Ra = 2 Ra_c, mixed against the FP64
+    GPU path, pencil resident on the device (as the headline's `value`).  Set-up, not
+    timed: the host assembly (kore_gb300.assembly_mac) and the onset search for Ra_c
+    (kore_gb300.onset, FP64 eigensolves on the device).  Parity as for the headline:
+    FP64 measurements, the rounding band and condition numbers (kore_gb300.conditioning)."""
+    import torch
+    from kore_gb300 import Pencil, kernel_launches, layout_from_params
+    from kore_gb300.assembly_mac import mac_params, mac_pencil_parts
+    from kore_gb300.onset import OnsetSearch
+    c = c or MAC[args.workload]
+    tau, nev, which = c["tau"], c["nev"], c["which"]
+    t0 = time.perf_counter()
+    A0, Ab, B, nrm = mac_pencil_parts(c["m"], c["symm"], c["Ek"], c["N"], c["lmax"], c["ricb"], Em=c["Em"],
+                                      Le2=c["Le2"], Prandtl=c["Prandtl"])
+    lay = layout_from_params(mac_params(c["m"], c["symm"], c["Ek"], c["N"], c["lmax"], c["ricb"]))
+    Bn = (B / nrm).tocsr()
+    t_asm = time.perf_counter() - t0
+    bv = -(c["Ek"] ** 2) / c["Prandtl"]      # buoyancy factor per unit Ra
+    t0 = time.perf_counter()
+    S = OnsetSearch(A0 / nrm, bv * Ab / nrm, 0.0, 1.0, Bn, lay, nev=16, which="TR", tau=0.0,
+                    precision="fp64", device=local)
+    Rac, wc = S.critical(c["log10_ra0"], dx=0.02, tol=1e-5, maxsteps=40)
+    t_onset = time.perf_counter() - t0
+    Ra = 2.0 * Rac
+    A = ((A0 + (Ra * bv) * Ab) / nrm).tocsr()
+    p = Pencil(A, Bn, layout=lay, device=local)
+    stream = torch.cuda.ExternalStream(p.stream(), device=torch.device("cuda", local))
+    steps = max(2, args.steps // 2)
+    spec = (tau, nev, which)
+    E64, lat64, pairs64, _ = time_arm(p, torch, stream, spec, "fp64", steps, 1, seed0=600)
+    l0 = kernel_launches()
+    E, lat, pairs, _ = time_arm(p, torch, stream, spec, "mixed", steps, 1, seed0=600)
+    launches = kernel_launches() - l0
+    lam, X = E.eigenvalues(), E.eigenvectors()
+    lam64, X64 = E64.eigenvalues(), E64.eigenvectors()
+    res = rel_residuals(A, Bn, lam[:nev], X[:, :nev])
+    res64 = rel_residuals(A, Bn, lam64[:nev], X64[:, :nev])
+    dists = np.array([np.min(np.abs(lam64 - l)) / abs(l) for l in lam[:nev]])
+    value = pairs / (sum(lat) / 1e3)
+    v64 = pairs64 / (sum(lat64) / 1e3)
+    out = {"metric": METRIC, "value": value, "unit": "eigenpairs/s", "ms_per_step": float(np.mean(lat)),
+           "config": {"workload": describe_mac(c), "n": int(lay.n), "blocks": int(lay.nblocks),
+                      "block": int(lay.block_sizes.max()), "l2": "inputs larger than L2",
+                      "parallelism": "replicas x1"},
+           "Ra_c": Rac, "omega_c": wc, "Ra": Ra, "onset_evaluations": S.evaluations,
+           "setup_s": {"assembly": t_asm, "onset_search": t_onset},
+           "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+           "fp64": {"value": v64, "p50_ms": float(np.percentile(lat64, 50)), "p99_ms": float(np.percentile(lat64, 99)),
+                    "max_eig_resid": float(res64.max()), "factor_s": E64.stats.get("factor_s"),
+                    "solver_stats": {k: E64.stats.get(k) for k in ("restarts", "op_applies", "sweeps")}},
+           "speedup_vs_fp64": value / v64, "max_eig_resid": float(res.max()),
+           "factor_s": E.stats.get("factor_s"),
+           "solver_stats": {k: E.stats.get(k) for k in ("restarts", "op_applies", "sweeps", "refine_iters_max")},
+           "max_rel_eig_diff_vs_fp64": float(dists.max()), "eigs_matching_fp64_1e-10": int((dists < 1e-10).sum()),
+           "gpu_launches": int(launches)}
+    if not args.no_parity:
+        out["parity"] = parity_block(A, Bn, lay, tau, nev, lam, X, None)
+    p.close()
+    if emit:
+        line = dict(out, n_gpus=1, steps=steps, warmup=1, higher_is_better=True, scaling="weak",
+                    vs_baseline=None, dtype="c64 factor + f64 refinement/Krylov",
+                    data="synthetic: pencil assembled from the kore parameters (restatement of the reference's "
+                         "dipole MAC assembly, matches it to 6e-16)")
+        print(json.dumps(line), flush=True)
+    return out
+
+
 SERVE = {
     "serve5": dict(pool=8, requests=120, rates=(2.0, 6.0), workers=4),
     # the summary carried on the headline line: one arrival rate
@@ -536,13 +623,15 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="shell2", choices=sorted(WORKLOADS) + sorted(FORCED) + sorted(SERVE))
+    ap.add_argument("--workload", default="shell2",
+                    choices=sorted(WORKLOADS) + sorted(FORCED) + sorted(SERVE) + sorted(MAC))
     ap.add_argument("--fp64-steps", type=int, default=None)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--no-forced", action="store_true", help="leave the batched forced-solve summary out")
     ap.add_argument("--no-serve", action="store_true", help="leave the serving summary out")
+    ap.add_argument("--no-mac", action="store_true", help="leave the dipole MAC summary out")
     ap.add_argument("--batch", type=int, default=4, help="targets of the batched form (1: skip it)")
     args = ap.parse_args()
 
@@ -559,6 +648,10 @@ def main():
     if args.workload in SERVE:
         if rank == 0:
             serve_bench(args, local)
+        return
+    if args.workload in MAC:
+        if rank == 0:
+            mac_bench(args, local)
         return
 
     import torch
@@ -585,7 +678,7 @@ def main():
         # the timed FP64 solves use the mixed arm's seeds (200, 201, ...), so that the last
         # of each starts from the same vector and their eigenvalues can be compared
         w64 = min(args.warmup, 1)
-        E64, lat64, pairs64, wall64 = time_arm(p, torch, stream, args.workload, "fp64", fsteps, w64,
+        E64, lat64, pairs64, wall64 = time_arm(p, torch, stream, (tau, nev, which), "fp64", fsteps, w64,
                                                seed0=200 + args.steps - fsteps - w64)
         lam64, X64 = E64.eigenvalues(), E64.eigenvectors()
         stats64 = dict(E64.stats)
@@ -674,8 +767,10 @@ def main():
         e2e = {"value": nev / (np.mean(ev_ms) / 1e3), "unit": "eigenpairs/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(ev_ms))}
 
-    # ---- configs 4 and 5 on the same line (their own sizes are in their config keys)
-    forced = serve = None
+    # ---- configs 3, 4 and 5 on the same line (their own sizes are in their config keys)
+    forced = serve = mac = None
+    if rank == 0 and not args.no_mac:
+        mac = mac_bench(args, local, MAC["mac3"], emit=False)
     if rank == 0 and not args.no_forced:
         forced = forced_bench(args, local, FORCED["forced4"], emit=False)
     if rank == 0 and not args.no_serve:
@@ -728,6 +823,7 @@ def main():
                                                            "max_resid", "fp64", "speedup_vs_fp64", "uneven",
                                                            "gpu_launches", "e2e")},
         "serving": serve and {k: serve[k] for k in ("metric", "value", "unit", "config", "rates")},
+        "mac_dipole": mac,
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)

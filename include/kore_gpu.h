@@ -84,11 +84,13 @@ typedef struct {
  * Krylov-Schur options: the fields bin/solve.py sets on SLEPc EPS
  * (setDimensions(nev) :96, setTolerances(tol, maxit) :97, setWhichEigenpairs :99-117,
  * setTarget(tau) :119) plus the explicit dimensions SLEPc would choose
- * (ncv = 0 -> min(n, max(2 nev, nev + 15)), as SLEPc's default).
+ * (ncv = 0 -> min(n, max(2 nev, nev + 15, min(64, 4 nev))): SLEPc's default raised
+ * to 4 nev, up to 64, because on the GPU a larger basis saves more operator
+ * applications than it costs).
  */
 typedef struct {
     int32_t nev;
-    int32_t ncv;          /* 0 = SLEPc default */
+    int32_t ncv;          /* 0 = default (see above) */
     double  tol;          /* relative, on the transformed eigenvalue theta */
     int32_t maxit;        /* restarts */
     int32_t which;        /* KORE_WHICH_TM, _TR or _TI: shift-and-invert needs a target

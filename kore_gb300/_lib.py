@@ -21,6 +21,13 @@ KORE_EPENDING = 9
 REQ_EIGEN, REQ_FORCED = 0, 1
 PREC = {"fp64": 0, "mixed": 1}
 WHICH = {"LM": 0, "SM": 1, "LR": 2, "SR": 3, "LI": 4, "SI": 5, "TM": 6, "TR": 7, "TI": 8}
+MAX_NCV = 64   # largest Krylov basis of the eigensolver
+
+
+def default_ncv(n, nev):
+    """The eigensolver's basis size when none is given (kore_eps_opts.ncv = 0): SLEPc's
+    max(2 nev, nev + 15), raised to 4 nev up to MAX_NCV."""
+    return min(int(n), max(2 * nev, nev + 15, min(MAX_NCV, 4 * nev)))
 
 # every function include/kore_gpu.h declares
 EXPORTS = ("kore_plan_create", "kore_factor", "kore_factor_shifts", "kore_solve", "kore_solve_dev",

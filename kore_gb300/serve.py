@@ -64,7 +64,7 @@ class Server:
                      vectors=False, key=None, refine_tol=0.0):
         """Eigensolve of data's pencil around `target` (kore_eigs); returns a ticket."""
         target = complex(target)
-        ncv_eff = ncv if ncv > 0 else min(data.n, max(2 * nev, nev + 15))
+        ncv_eff = ncv if ncv > 0 else L.default_ncv(data.n, nev)
         evals = np.zeros(ncv_eff, dtype=np.complex128)
         evecs = np.zeros((ncv_eff, data.n), dtype=np.complex128) if vectors else None
         nconv = C.c_int32(0)

@@ -236,7 +236,7 @@ def eigs_targets(pencil, targets, nev, which="TM", precision="mixed", tol=1e-15,
     mx = 0
     for t in range(T):
         k = int(nevs[t])
-        m = int(ncv) or min(pencil.n, max(2 * k, k + 15))
+        m = int(ncv) or L.default_ncv(pencil.n, k)
         mx = max(mx, m)
         opts[t] = L.EpsOpts(nev=k, ncv=int(ncv), tol=tol, maxit=maxit, which=L.WHICH[which], target_re=tg[t].real,
                             target_im=tg[t].imag, seed=int(sds[t]), purify=int(purify),
@@ -349,7 +349,7 @@ class EPS:
 
     def getDimensions(self):
         n = self.pencil.n
-        ncv = self.ncv or min(n, max(2 * self.nev, self.nev + 15))
+        ncv = self.ncv or L.default_ncv(n, self.nev)
         return self.nev, ncv, ncv
 
     def getTolerances(self):

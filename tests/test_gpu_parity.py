@@ -9,7 +9,7 @@ pytestmark = pytest.mark.gpu
 
 SPINOVER_GOLDEN = np.array([-1.019947097016500742e-01, 1.005733690103750355e+00])
 
-SOLVE_CASES = ["shell_m1_ek1e-4", "spinover", "jones2000_rac", "dormy2004_rac", "mac_dipole_small",
+SOLVE_CASES = ["shell_m1_ek1e-4", "spinover", "jones2000_rac", "dormy2004_rac", "mac_dipole_small", "mac_dipole_medium",
                "mac_quadrupole_small", "shell_m2_small"]
 
 
@@ -139,7 +139,8 @@ def test_eigs_convective_onset(gpu_lib, case, name, omega_c):
 
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-10)])
-@pytest.mark.parametrize("name", ["mac_dipole_small", "mac_quadrupole_small", "shell_m2_small"])
+@pytest.mark.parametrize("name", ["mac_dipole_small", "mac_dipole_medium", "mac_dipole_internal",
+                                  "mac_quadrupole_small", "shell_m2_small"])
 def test_eigs_other_pencils(gpu_lib, case, name, precision, tol):
     """Magneto-Archimedes-Coriolis pencils (dipole: superblocks {upol, btor, theta} /
     {utor, bpol}; quadrupole: degree pairs merged for the l +- 2 coupling) and an m=2
