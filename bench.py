@@ -308,6 +308,35 @@ def parity_block(A, B, lay, tau, nev, lam, X, batched):
     return out
 
 
+def tracking_bench(A, B, lay, local, tau, nev, which, steps=10, spacing=0.004j, radius=0.05):
+    """A target followed along the imaginary axis (parameter tracking: tau, tau + spacing,
+    ...), one served eigen request at a time on one pencil, mixed precision.  Without
+    reuse every request factorises its target; with `radius` a request runs on the cached
+    factors of the previous shift within that distance, started from the eigenvectors the
+    slot returned last.  Latency is the serving queue's run time of each request."""
+    from kore_gb300.serve import PencilData, Server
+    P = PencilData(A, B, layout=lay)
+    out = {"targets": [[float(tau.real), float(tau.imag)], [float(spacing.real), float(spacing.imag)], steps],
+           "nev": nev}
+    for name, r in (("fresh", 0.0), ("reuse", radius)):
+        lat, reused, warm, applies, resid = [], 0, 0, [], []
+        with Server(workers=1, device=local) as srv:
+            for k in range(steps):
+                res = srv.result(srv.submit_eigen(P, tau + k * spacing, nev, which, seed=900 + k,
+                                                  reuse_radius=r, vectors=True))
+                lat.append(res["run_ms"])
+                st = res["stats"]
+                reused += st["factor_reused"]
+                warm += st["warm_started"]
+                applies.append(st["op_applies"])
+                resid.append(float(rel_residuals(A, B, res["evals"][:nev], res["evecs"][:, :nev]).max()))
+        out[name] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                     "mean_ms": float(np.mean(lat)), "factor_reused": reused, "warm_started": warm,
+                     "op_applies_mean": float(np.mean(applies)), "max_eig_resid": max(resid)}
+    out["speedup_mean_latency"] = out["fresh"]["mean_ms"] / out["reuse"]["mean_ms"]
+    return out
+
+
 def uneven_instances(count, seed=7):
     """Uneven forced problems drawn from the sweep's ranges: m in 1..8 (forcing 10 acts on
     l = m, so m = 0 has no forcing), N even in [64, 320], lmax in [60, 400] with
@@ -632,6 +661,7 @@ def main():
     ap.add_argument("--no-forced", action="store_true", help="leave the batched forced-solve summary out")
     ap.add_argument("--no-serve", action="store_true", help="leave the serving summary out")
     ap.add_argument("--no-mac", action="store_true", help="leave the dipole MAC summary out")
+    ap.add_argument("--no-track", action="store_true", help="leave the target-tracking serving summary out")
     ap.add_argument("--batch", type=int, default=4, help="targets of the batched form (1: skip it)")
     args = ap.parse_args()
 
@@ -768,7 +798,9 @@ def main():
                "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(ev_ms))}
 
     # ---- configs 3, 4 and 5 on the same line (their own sizes are in their config keys)
-    forced = serve = mac = None
+    forced = serve = mac = track = None
+    if rank == 0 and not args.no_track:
+        track = tracking_bench(A, B, lay, local, tau, nev, which)
     if rank == 0 and not args.no_mac:
         mac = mac_bench(args, local, MAC["mac3"], emit=False)
     if rank == 0 and not args.no_forced:
@@ -824,6 +856,7 @@ def main():
                                                            "gpu_launches", "e2e")},
         "serving": serve and {k: serve[k] for k in ("metric", "value", "unit", "config", "rates")},
         "mac_dipole": mac,
+        "serving_tracking": track,
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)

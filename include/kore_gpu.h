@@ -95,13 +95,27 @@ typedef struct {
     int32_t maxit;        /* restarts */
     int32_t which;        /* KORE_WHICH_TM, _TR or _TI: shift-and-invert needs a target
                              criterion (SLEPc refuses the others under sinvert) */
-    double  target_re, target_im;   /* tau; must equal the factorised shift */
+    double  target_re, target_im;   /* tau: `which` measures distances from it */
     uint64_t seed;        /* start vector: complex standard normal from this seed */
     int32_t purify;       /* applications of OP to each eigenvector before it is
                              returned: 1 is SLEPc's default purification, 0 none */
     double  refine_tol;   /* mixed precision: relative residual of each OP application
                              (<= 0 selects 1e-16); the purifying application of the
                              eigenvectors is refined until the residual stops decreasing */
+    /* Spectral-transformation shift sigma (SLEPc's -st_shift): OP = (A - sigma B)^-1 B and
+     * lambda = sigma + 1/theta, while `which` still measures from the target.  has_shift = 0:
+     * sigma is the target (SLEPc's default).  The factorised shift must equal sigma. */
+    double  shift_re, shift_im;
+    int32_t has_shift;
+    /* 1: start from the normalised sum of the eigenvectors the previous target in the same
+     * slot returned (the plan keeps one such vector per slot), when there is one, instead
+     * of the seeded vector.  The result then depends on that earlier solve. */
+    int32_t warm;
+    /* Batched and served eigensolves (kore_eigs_shifts, the serving queue): > 0 lets a target
+     * run on an idle slot whose factorised shift lies within this distance of the target,
+     * as sigma of that slot, without re-factorising, and started warm.  0: only a slot
+     * holding exactly the target's shift is reused. */
+    double  reuse_radius;
 } kore_eps_opts;
 
 /* Per-call statistics, filled by kore_eigs / kore_solve when the pointer is non-NULL. */
@@ -113,6 +127,9 @@ typedef struct {
     int32_t refine_iters_max;  /* mixed precision: worst refinement count of one application */
     double  solve_resid_max;   /* worst relative residual of one application */
     double  factor_ms, iterate_ms;
+    int32_t factor_reused;     /* eigen: the slot already held the factors of the shift used */
+    int32_t warm_started;      /* eigen: started from the slot's last eigenvectors (opts.warm) */
+    double  shift_re, shift_im;   /* eigen: the shift of the spectral transformation used */
 } kore_stats;
 
 /* Replaces bin/solve.py:40-86 (load_csr + PETSc Mat assembly of A and B). */
@@ -276,6 +293,7 @@ typedef struct {
     int32_t max_pairs;
     int32_t *nconv;                   /* eigen: converged pairs */
     double *timing_ms;                /* NULL or 3 doubles: queued, running, submit to finish */
+    kore_stats *stats;                /* eigen: NULL or the solve's statistics */
 } kore_request;
 
 /* hbm_budget <= 0: 90% of the device's free memory at creation. */

@@ -76,6 +76,11 @@ class EpsOpts(C.Structure):
         ("seed", C.c_uint64),
         ("purify", C.c_int32),
         ("refine_tol", C.c_double),
+        ("shift_re", C.c_double),
+        ("shift_im", C.c_double),
+        ("has_shift", C.c_int32),
+        ("warm", C.c_int32),
+        ("reuse_radius", C.c_double),
     ]
 
 
@@ -89,6 +94,10 @@ class Stats(C.Structure):
         ("solve_resid_max", C.c_double),
         ("factor_ms", C.c_double),
         ("iterate_ms", C.c_double),
+        ("factor_reused", C.c_int32),
+        ("warm_started", C.c_int32),
+        ("shift_re", C.c_double),
+        ("shift_im", C.c_double),
     ]
 
     def as_dict(self):
@@ -113,6 +122,7 @@ class Request(C.Structure):
         ("max_pairs", C.c_int32),
         ("nconv", C.POINTER(C.c_int32)),
         ("timing_ms", C.c_void_p),
+        ("stats", C.c_void_p),
     ]
 
 

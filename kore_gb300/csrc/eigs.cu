@@ -48,10 +48,12 @@ __host__ __device__ inline double lambda_key(double2 lam, int which, double tre,
     }
     return 0.0;
 }
-// The same key for a Ritz value theta of OP = (A - tau B)^-1 B: lambda = tau + 1/theta.
-__host__ __device__ inline double which_key(double2 theta, int which, double tre, double tim) {
+// The same key for a Ritz value theta of OP = (A - sigma B)^-1 B: lambda = sigma + 1/theta,
+// measured from the target tau.
+__host__ __device__ inline double which_key(double2 theta, int which, double sre, double sim, double tre,
+                                            double tim) {
     const double d = theta.x * theta.x + theta.y * theta.y;
-    const double2 lam = (d > 0.0) ? mk(tre + theta.x / d, tim - theta.y / d) : mk(INFINITY, 0.0);
+    const double2 lam = (d > 0.0) ? mk(sre + theta.x / d, sim - theta.y / d) : mk(INFINITY, 0.0);
     return lambda_key(lam, which, tre, tim);
 }
 
@@ -157,7 +159,8 @@ __device__ __forceinline__ void apply_rot(double2 *H, double2 *Q, int m, int k, 
 struct SchurBatch {
     unsigned mask;
     int m[kMaxTargets], which[kMaxTargets];
-    double tre[kMaxTargets], tim[kMaxTargets];
+    double tre[kMaxTargets], tim[kMaxTargets];   // targets
+    double sre[kMaxTargets], sim[kMaxTargets];   // shifts of the slots' factors
     int64_t hstride, sqstride, vstride;
 };
 
@@ -170,7 +173,7 @@ __global__ void __launch_bounds__(kSchurT) k_schur(const double2 *__restrict__ H
     const int tg = blockIdx.x;
     if (!((sb.mask >> tg) & 1u)) return;
     const int m = sb.m[tg], which = sb.which[tg];
-    const double tre = sb.tre[tg], tim = sb.tim[tg];
+    const double tre = sb.tre[tg], tim = sb.tim[tg], sre = sb.sre[tg], sim = sb.sim[tg];
     const double2 *Hbar = Hbar0 + tg * sb.hstride;
     const SchurOut out{out0.T + tg * sb.sqstride, out0.Q + tg * sb.sqstride, out0.Y + tg * sb.sqstride,
                        out0.theta + tg * sb.vstride, out0.est + tg * sb.vstride, out0.bnew + tg * sb.vstride,
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(kSchurT) k_schur(const double2 *__restrict__ H
     __syncthreads();
 
     // --- order the diagonal by the `which` key: selection by adjacent swaps (Givens)
-    for (int j = tid; j < m; j += kSchurT) key[j] = which_key(H[j + j * m], which, tre, tim);
+    for (int j = tid; j < m; j += kSchurT) key[j] = which_key(H[j + j * m], which, sre, sim, tre, tim);
     __syncthreads();
     for (int pos = 0; pos < m; ++pos) {
         int best = pos;
@@ -580,6 +583,15 @@ __global__ void k_scale_copy(int64_t np, TVec src, const double *__restrict__ be
 }
 
 // dst_t = src_t (np entries)
+// out = sum of the n columns of V (column k at V + k * np)
+__global__ void k_sum_cols(int64_t np, const double2 *__restrict__ V, int n, double2 *__restrict__ out) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < np; r += (int64_t)gridDim.x * blockDim.x) {
+        double2 s = mk(0.0, 0.0);
+        for (int k = 0; k < n; ++k) s = s + V[(int64_t)k * np + r];
+        out[r] = s;
+    }
+}
+
 __global__ void k_copy_vecs(int64_t np, TVec src, TVec dst, unsigned mask) {
     const int tg = blockIdx.y;
     if (!in_mask(mask, tg)) return;
@@ -853,6 +865,11 @@ struct Run {
 // the projected problem of a larger basis, and the larger basis needs fewer restarts and
 // fewer applications: on the 240k-unknown shell at nev = 16, 64 vectors take 191
 // applications and 5 restarts against 303-350 and 22-26 with 32.
+// The shift of the spectral transformation: the target unless set apart (SLEPc -st_shift).
+inline double2 shift_of(const kore_eps_opts &o) {
+    return o.has_shift ? mk(o.shift_re, o.shift_im) : mk(o.target_re, o.target_im);
+}
+
 int ncv_of(const kore_plan *p, const kore_eps_opts &o) {
     if (o.ncv > 0) return o.ncv;
     const int m = std::max(std::max(2 * o.nev, o.nev + 15), std::min(kMaxNcv, 4 * o.nev));
@@ -861,7 +878,8 @@ int ncv_of(const kore_plan *p, const kore_eps_opts &o) {
 
 // KORE_OK when the options can run in a slot of this engine
 int check_opts(const kore_plan *p, const kore_eps_opts &o, int M) {
-    if (o.nev <= 0 || o.purify < 0) return KORE_EINVAL;
+    if (o.nev <= 0 || o.purify < 0 || !(o.reuse_radius >= 0.0)) return KORE_EINVAL;
+    if (o.has_shift && !(std::isfinite(o.shift_re) && std::isfinite(o.shift_im))) return KORE_EINVAL;
     // shift-and-invert needs a target criterion: SLEPc's EPSSetUp refuses the others
     // under -st_type sinvert, the only spectral transformation of the kore path
     if (o.which != KORE_WHICH_TM && o.which != KORE_WHICH_TR && o.which != KORE_WHICH_TI) return KORE_EINVAL;
@@ -877,10 +895,11 @@ int start_target(Run &r, int s, const EigsTarget &t) {
     Ctx &c = r.c;
     const kore_eps_opts &ot = t.opts;
     Slot &x = r.sl[s];
-    const bool reuse = x.valid && p->sigmas[s].x == ot.target_re && p->sigmas[s].y == ot.target_im;
+    const double2 sh = shift_of(ot);
+    const bool reuse = x.valid && p->sigmas[s].x == sh.x && p->sigmas[s].y == sh.y;
     if (!reuse) {
         x.valid = false;
-        KORE_TRY(kore_factor_slot(p, s, ot.target_re, ot.target_im));
+        KORE_TRY(kore_factor_slot(p, s, sh.x, sh.y));
         x.valid = true;
     }
     x.busy = true;
@@ -892,12 +911,22 @@ int start_target(Run &r, int s, const EigsTarget &t) {
     x.j = 0; x.restarts = 0; x.nconv = 0; x.applies = 0;
     x.nout = 0; x.k = 0; x.pstep = 0;
     r.sb.m[s] = x.m; r.sb.which[s] = ot.which; r.sb.tre[s] = ot.target_re; r.sb.tim[s] = ot.target_im;
-    // start vector (original order) -> padded -> normalised column 0
-    std::vector<double2> hv((size_t)p->n);
-    start_vector(p->n, ot.seed, hv.data());
+    r.sb.sre[s] = sh.x; r.sb.sim[s] = sh.y;
+    // start vector: the slot's warm vector, or seeded (original order) -> padded; then
+    // normalised into column 0
     double2 *orig = c.xin + (int64_t)s * c.np, *pad = c.w + (int64_t)s * c.np;
-    KORE_CUDA_TRY(cudaMemcpyAsync(orig, hv.data(), hv.size() * sizeof(double2), cudaMemcpyHostToDevice, p->stream));
-    KORE_TRY(kore_gather(p, orig, pad));
+    std::vector<double2> hv;
+    if (ot.warm && s < (int)p->warm_ok.size() && p->warm_ok[s]) {
+        KORE_CUDA_TRY(cudaMemcpyAsync(pad, p->d_warm + (int64_t)s * c.np, c.np * sizeof(double2),
+                                      cudaMemcpyDeviceToDevice, p->stream));
+        x.tgt.warm_started = 1;
+    } else {
+        hv.resize((size_t)p->n);
+        start_vector(p->n, ot.seed, hv.data());
+        KORE_CUDA_TRY(cudaMemcpyAsync(orig, hv.data(), hv.size() * sizeof(double2), cudaMemcpyHostToDevice,
+                                      p->stream));
+        KORE_TRY(kore_gather(p, orig, pad));
+    }
     TCols tc{};
     tc.mask = 1u << s;
     tc.n[s] = 0; tc.j[s] = -1; tc.ld[s] = x.m + 1;
@@ -929,10 +958,25 @@ int fill_slots(Run &r) {
             continue;
         }
         int s = -1;
+        const double2 sh = shift_of(t.opts);
         for (int u = 0; u < r.T && s < 0; ++u)
-            if (!r.sl[u].busy && r.sl[u].valid && r.p->sigmas[u].x == t.opts.target_re &&
-                r.p->sigmas[u].y == t.opts.target_im)
-                s = u;
+            if (!r.sl[u].busy && r.sl[u].valid && r.p->sigmas[u].x == sh.x && r.p->sigmas[u].y == sh.y) s = u;
+        if (s < 0 && t.opts.reuse_radius > 0.0 && !t.opts.has_shift) {
+            // the idle slot whose factors lie nearest the target, within the radius: run
+            // there with that slot's shift, started from its last eigenvectors
+            double best = t.opts.reuse_radius;
+            for (int u = 0; u < r.T; ++u)
+                if (!r.sl[u].busy && r.sl[u].valid) {
+                    const double d = hypot(r.p->sigmas[u].x - t.opts.target_re, r.p->sigmas[u].y - t.opts.target_im);
+                    if (d <= best) { best = d; s = u; }
+                }
+            if (s >= 0) {
+                t.opts.has_shift = 1;
+                t.opts.shift_re = r.p->sigmas[s].x;
+                t.opts.shift_im = r.p->sigmas[s].y;
+                t.opts.warm = 1;
+            }
+        }
         for (int u = 0; u < r.T && s < 0; ++u)
             if (!r.sl[u].busy) s = u;
         const int st = start_target(r, s, t);
@@ -966,7 +1010,8 @@ int finish_target(Run &r, int s) {
             // B x = 0 or a NaN: keep the back-transformed Ritz value
             const double2 th = x.theta[k];
             const double d = th.x * th.x + th.y * th.y;
-            lam[k] = mk(ot.target_re + th.x / d, ot.target_im - th.y / d);
+            const double2 sh = shift_of(ot);
+            lam[k] = mk(sh.x + th.x / d, sh.y - th.y / d);
         }
     std::vector<int> order(x.nout);
     std::vector<double> key(x.nout);
@@ -996,6 +1041,17 @@ int finish_target(Run &r, int s) {
         q.solve_resid_max = irs.eta_max;
         q.sweeps = irs0.sweeps;   // sweep launches of the engine so far (counted in shift 0's state)
         q.iterate_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - r.t0).count();
+        q.factor_reused = t.reused;
+        q.warm_started = t.warm_started;
+        q.shift_re = shift_of(ot).x;
+        q.shift_im = shift_of(ot).y;
+    }
+    // the slot's warm vector for a later target: the sum of the eigenvectors just returned
+    if (x.nout > 0 && x.nconv > 0 && s < p->warm_cap) {
+        k_sum_cols<<<c.grid, 256, 0, p->stream>>>(c.np, x.Vt, x.nout, p->d_warm + (int64_t)s * c.np);
+        KORE_LAUNCHED(1);
+        KORE_CUDA_TRY(cudaGetLastError());
+        p->warm_ok[s] = 1;
     }
     x.busy = false;
     x.phase = 2;
@@ -1118,6 +1174,14 @@ int kore_eigs_engine(kore_plan *p, EigsSource *src, bool *valid, int max_ncv) {
         KORE_TRY(kore_alloc(p, (void **)&p->d_Vtmp, (size_t)np * vcols * sizeof(double2)));
         KORE_TRY(kore_alloc(p, (void **)&p->d_ksx, (size_t)np * T * sizeof(double2)));
         p->ks_cap = vcols;
+    }
+    if (p->warm_cap < T) {
+        cudaFree(p->d_warm);
+        p->d_warm = nullptr;
+        p->warm_cap = 0;
+        p->warm_ok.assign(T, 0);
+        KORE_TRY(kore_alloc(p, (void **)&p->d_warm, (size_t)np * T * sizeof(double2)));
+        p->warm_cap = T;
     }
     if (p->ks_small_cap < T) {
         cudaFree(p->d_small);
@@ -1296,7 +1360,7 @@ int kore_eigs_impl(kore_plan *p, int ntarget, const kore_eps_opts *o, double *ev
     if (!o || T < 1 || T > kMaxTargets || ntarget < T) return KORE_EINVAL;
     for (int t = 0; t < ntarget; ++t) {
         KORE_TRY(check_opts(p, o[t], kMaxNcv));
-        if (t < T && (o[t].target_re != p->sigmas[t].x || o[t].target_im != p->sigmas[t].y)) return KORE_EINVAL;
+        if (t < T && (shift_of(o[t]).x != p->sigmas[t].x || shift_of(o[t]).y != p->sigmas[t].y)) return KORE_EINVAL;
     }
     ArraySource src;
     src.o = o; src.ntarget = ntarget; src.max_pairs = max_pairs; src.n = p->n;

@@ -15,7 +15,7 @@ struct IrState {
     int sweeps;        // sweeps that ran
     int pad_;
     double prev;       // previous eta of the current application
-    double eta_max;    // worst final eta
+    double eta_max;    // worst final eta (an application that ran out of corrections: its last measured eta)
     int sweeps_total;  // sweeps that ran since the plan was created (kept by kore_ir_reset)
     int pad2_;
 };
@@ -151,6 +151,11 @@ struct kore_plan {
     int64_t ks_cap = 0;               // columns of d_V, d_Vtmp
     double2 *d_small = nullptr;       // projected problems, Gram-Schmidt coefficients and partial sums
     int ks_small_cap = 0;             // targets d_small holds
+    // warm starts: per slot, the sum of the eigenvectors its last target returned (padded
+    // order), kept across eigensolves of the plan
+    double2 *d_warm = nullptr;        // np x warm_cap
+    int warm_cap = 0;
+    std::vector<char> warm_ok;        // slot s holds such a vector
 
     size_t bytes = 0;
     size_t factor_bytes = 0;          // bytes of the per-shift buffers
@@ -236,6 +241,7 @@ struct EigsTarget {
     kore_stats *stats = nullptr;   // may be NULL
     void *tag = nullptr;           // the source's handle of the target
     int reused = 0;                // set by the engine: the slot already held this shift's factors
+    int warm_started = 0;          // set by the engine: started from the slot's warm vector
 };
 // Supplier of targets to kore_eigs_engine (called from the engine's thread).
 struct EigsSource {

@@ -95,7 +95,7 @@ void free_plan(kore_plan *p) {
     void *ptrs[] = {p->d_arow, p->d_acol, p->d_asplit, p->d_aval, p->d_brow, p->d_bcol, p->d_bval,
                     p->d_slot2orig, p->d_bsz, p->d_Dinv, p->d_Gm, p->d_Hm, p->d_Dw, p->d_LU, p->d_lev,
                     p->d_rscale, p->d_T, p->d_piv, p->d_pidx, p->d_used, p->d_zlo, p->d_xlo, p->d_flo,
-                    p->d_red, p->d_part, p->d_err, p->d_bar, p->d_ir, p->d_V, p->d_Vtmp, p->d_ksx, p->d_small,
+                    p->d_red, p->d_part, p->d_err, p->d_bar, p->d_ir, p->d_V, p->d_Vtmp, p->d_ksx, p->d_small, p->d_warm,
                     p->d_sigma, p->d_minf, p->d_bb, p->d_xb, p->d_rb, p->d_bn, p->d_rn, p->d_cnt,
                     p->d_ell_col, p->d_ell_src, p->d_ell_val, p->d_long_rows, p->d_srow, p->d_smid,
                     p->d_scol, p->d_sval, p->d_cc_ptr, p->d_cc_row, p->d_cc_src};

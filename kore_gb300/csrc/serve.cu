@@ -199,7 +199,7 @@ struct ServeSource : EigsSource {
         t->evecs = r.evecs;
         t->max_pairs = r.max_pairs;
         t->nconv = r.nconv;
-        t->stats = nullptr;
+        t->stats = r.stats;
         t->tag = q;
     }
     bool next(EigsTarget *t) override {

@@ -1039,6 +1039,9 @@ __global__ void k_ir_end(IrState *st, int nshift) {
     const int s = threadIdx.x;
     if (s >= nshift) return;
     if (st[s].iters_cur > st[s].iters_max) st[s].iters_max = st[s].iters_cur;
+    // the loop ran out of corrections before the test passed: report the last measured
+    // eta (taken before the final correction, so an upper estimate)
+    if (!st[s].done && st[s].iters_cur > 0) st[s].eta_max = fmax(st[s].eta_max, st[s].prev);
     st[s].iters_cur = 0;
 }
 

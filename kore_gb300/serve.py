@@ -61,8 +61,14 @@ class Server:
         return t.value
 
     def submit_eigen(self, data, target, nev, which="TM", tol=1e-15, maxit=50, ncv=0, precision="mixed", seed=1,
-                     vectors=False, key=None, refine_tol=0.0):
-        """Eigensolve of data's pencil around `target` (kore_eigs); returns a ticket."""
+                     vectors=False, key=None, refine_tol=0.0, reuse_radius=0.0):
+        """Eigensolve of data's pencil around `target` (kore_eigs); returns a ticket.
+
+        reuse_radius > 0: when an idle slot of the pencil's cached plan holds factors at a
+        shift within this distance of the target, the request runs there with that shift
+        (no re-factorisation; eigenvalues still sorted from the target) and starts from the
+        eigenvectors that slot returned last.  Its result then depends on that earlier
+        request, within the solver's tolerance."""
         target = complex(target)
         ncv_eff = ncv if ncv > 0 else L.default_ncv(data.n, nev)
         evals = np.zeros(ncv_eff, dtype=np.complex128)
@@ -76,15 +82,18 @@ class Server:
         r.precision = L.PREC[precision]
         r.sigma_re, r.sigma_im = target.real, target.imag
         r.opts = L.EpsOpts(nev=nev, ncv=ncv, tol=tol, maxit=maxit, which=L.WHICH[which], target_re=target.real,
-                           target_im=target.imag, seed=seed, purify=1, refine_tol=refine_tol)
+                           target_im=target.imag, seed=seed, purify=1, refine_tol=refine_tol,
+                           reuse_radius=float(reuse_radius))
         r.evals = evals.ctypes.data
         r.evecs = evecs.ctypes.data if vectors else None
         r.max_pairs = ncv_eff
         r.nconv = C.pointer(nconv)
         r.timing_ms = timing.ctypes.data
-        keep = (data, evals, evecs, nconv, timing)
+        st = L.Stats()
+        r.stats = C.addressof(st)
+        keep = (data, evals, evecs, nconv, timing, st)
         return self._submit(r, keep, {"kind": "eigen", "evals": evals, "evecs": evecs, "nconv": nconv,
-                                      "timing": timing, "target": target})
+                                      "timing": timing, "target": target, "stats_struct": st})
 
     def submit_forced(self, data, sigma, rhs, scale=1.0, precision="mixed", refine_tol=0.0, key=None):
         """x = (A - sigma B)^-1 rhs / scale (kore_solve); returns a ticket."""
@@ -124,6 +133,8 @@ class Server:
         if res["kind"] == "eigen":
             k = res["nconv"].value
             out["nconv"] = k
+            st = out.pop("stats_struct")
+            out["stats"] = st.as_dict()
             out["evals"] = res["evals"][:k]
             if res["evecs"] is not None:
                 out["evecs"] = res["evecs"][:k].T

@@ -211,7 +211,7 @@ def forced_sweep(pencil, omegas, b, precision="mixed", group=16, refine_tol=0.0,
 
 
 def eigs_targets(pencil, targets, nev, which="TM", precision="mixed", tol=1e-15, maxit=50, seeds=None, ncv=0,
-                 purify=True, refine_tol=0.0, vectors=True, slots=None):
+                 purify=True, refine_tol=0.0, vectors=True, slots=None, reuse_radius=0.0):
     """Shift-and-invert Krylov-Schur at several targets of one pencil, the targets
     stepping together in shared launches (``kore_eigs_shifts``).  ``slots`` targets run
     at a time (default: all); when one finishes, the next takes its slot (its shift is
@@ -223,6 +223,11 @@ def eigs_targets(pencil, targets, nev, which="TM", precision="mixed", tol=1e-15,
     in SLEPc's order for ``which`` and their unit eigenvectors.  ``nev`` and ``seeds``
     may be one value or one per target.  Factorises ``A - tau_t B`` for every target
     first (one batched factorisation).
+
+    ``reuse_radius`` > 0: a later target runs on an idle slot whose shift lies within this
+    distance of it (that shift is the spectral transformation's, the eigenvalues are still
+    sorted from the target), without re-factorising, started from the eigenvectors the
+    slot returned last.
 
     Returns a list of (eigenvalues, eigenvectors or None, stats dict), one per target.
     """
@@ -240,7 +245,7 @@ def eigs_targets(pencil, targets, nev, which="TM", precision="mixed", tol=1e-15,
         mx = max(mx, m)
         opts[t] = L.EpsOpts(nev=k, ncv=int(ncv), tol=tol, maxit=maxit, which=L.WHICH[which], target_re=tg[t].real,
                             target_im=tg[t].imag, seed=int(sds[t]), purify=int(purify),
-                            refine_tol=refine_tol)
+                            refine_tol=refine_tol, reuse_radius=float(reuse_radius))
     ev = np.zeros((T, mx), dtype=np.complex128)
     X = np.zeros((T, mx, pencil.n), dtype=np.complex128) if vectors else None
     nconv = (C.c_int * T)()
@@ -279,6 +284,7 @@ class EPS:
         self.tol, self.maxit = 1e-8, 100
         self.which = "LM"
         self.target = 0j
+        self.shift = None          # spectral-transformation shift (SLEPc -st_shift); None: the target
         self.st_type = "sinvert"
         self.precision = "fp64"
         self.seed = 0
@@ -346,6 +352,14 @@ class EPS:
             self.seed = int(o["kore_seed"])
         if "kore_refine_tol" in o:
             self.refine_tol = float(o["kore_refine_tol"])
+        if "st_shift" in o:
+            self.shift = complex(o["st_shift"])
+
+    def setShift(self, sigma):
+        """Shift of the spectral transformation, apart from the target (SLEPc's
+        ST.setShift / -st_shift): OP = (A - sigma B)^-1 B, eigenvalues sorted by `which`
+        from the target."""
+        self.shift = None if sigma is None else complex(sigma)
 
     def getDimensions(self):
         n = self.pencil.n
@@ -366,12 +380,14 @@ class EPS:
         if self.which not in ("TM", "TR", "TI"):
             # SLEPc's EPSSetUp stops here under -st_type sinvert, the kore path's transformation
             raise ValueError(f"shift-and-invert requires a target 'which' (TM, TR or TI), not {self.which!r}")
-        if p.sigma != self.target or p.precision != self.precision:
-            p.factor(self.target, self.precision)
+        sigma = self.target if self.shift is None else self.shift
+        if p.sigma != sigma or p.precision != self.precision:
+            p.factor(sigma, self.precision)
         nev, ncv, _ = self.getDimensions()
         o = L.EpsOpts(nev=nev, ncv=ncv, tol=self.tol, maxit=self.maxit, which=L.WHICH[self.which],
                       target_re=self.target.real, target_im=self.target.imag, seed=self.seed,
-                      purify=self.purify_steps if self.purify else 0, refine_tol=self.refine_tol)
+                      purify=self.purify_steps if self.purify else 0, refine_tol=self.refine_tol,
+                      shift_re=sigma.real, shift_im=sigma.imag, has_shift=int(self.shift is not None))
         ev = np.zeros(ncv, dtype=np.complex128)
         X = np.zeros((ncv, p.n), dtype=np.complex128)
         nconv = C.c_int(0)

@@ -93,3 +93,33 @@ def test_mac_pencil_is_affine_in_rayleigh_number():
         A, B2 = mac_pencil(1, -1, 1e-3, 20, 12, 0.35, Ra=Ra, **kw)
         assert ssl.norm(A - (A0 - Ra * 1e-6 * Ab) / nrm) <= 1e-15 * ssl.norm(A)
         assert ssl.norm(B2 - B / nrm) == 0.0
+
+
+def test_fullsize_bench_pencil_matches_reference_fingerprint():
+    """The 240,000-unknown benchmark pencil (m=2, Ek=1e-7, N=400, lmax=601) built by the
+    restatement against the reference's own assembly of it, through the fingerprint
+    tests/golden/make_fullsize_fingerprint.py stored: norms, nonzero counts, and 4096
+    seeded rows of A v and B v for a seeded v."""
+    import json
+    import os
+    import sys
+    from conftest import GOLDEN
+    path = os.path.join(GOLDEN, "shell2_fingerprint.npz")
+    z = np.load(path)
+    meta = json.loads(str(z["meta"]))
+    sys.path.insert(0, GOLDEN)
+    from make_fullsize_fingerprint import fingerprint
+    A, B = hydro_pencil(meta["m"], meta["symm"], meta["Ek"], meta["N"], meta["lmax"], meta["ricb"])
+    f = fingerprint(A, B)
+    assert tuple(f["shape"]) == tuple(z["shape"])
+    assert np.array_equal(f["rows"], z["rows"])
+    assert abs(f["A_fro"] - float(z["A_fro"])) <= 1e-14 * float(z["A_fro"])
+    assert abs(f["B_fro"] - float(z["B_fro"])) <= 1e-14 * float(z["B_fro"])
+    # rows of A v and B v, relative to the row's 1-norm times max |v| (~5 for this v)
+    scale_a = z["A_row1"] * 6.0
+    scale_b = np.maximum(z["B_row1"], 1e-300) * 6.0
+    assert np.all(np.abs(f["Av"] - z["Av"]) <= 1e-13 * scale_a)
+    assert np.all(np.abs(f["Bv"] - z["Bv"]) <= 1e-13 * scale_b)
+    assert np.allclose(f["A_row1"], z["A_row1"], rtol=1e-13, atol=0)
+    # explicit zeros aside, the sparsity matches
+    assert abs(int(f["A_nnz"]) - int(z["A_nnz"])) <= 0.001 * int(z["A_nnz"])
