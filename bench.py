@@ -308,21 +308,22 @@ def parity_block(A, B, lay, tau, nev, lam, X, batched):
     return out
 
 
-def tracking_bench(A, B, lay, local, tau, nev, which, steps=10, spacing=0.004j, radius=0.05):
+def tracking_bench(A, B, lay, local, tau, nev, which, steps=8, spacing=0.004j, radius=0.01):
     """A target followed along the imaginary axis (parameter tracking: tau, tau + spacing,
-    ...), one served eigen request at a time on one pencil, mixed precision.  Without
+    ...), one served eigen request at a time on one pencil, in both precisions.  Without
     reuse every request factorises its target; with `radius` a request runs on the cached
-    factors of the previous shift within that distance, started from the eigenvectors the
-    slot returned last.  Latency is the serving queue's run time of each request."""
+    factors of a shift within that distance.  Latency is the serving queue's run time of
+    each request."""
     from kore_gb300.serve import PencilData, Server
     P = PencilData(A, B, layout=lay)
     out = {"targets": [[float(tau.real), float(tau.imag)], [float(spacing.real), float(spacing.imag)], steps],
-           "nev": nev}
-    for name, r in (("fresh", 0.0), ("reuse", radius)):
+           "nev": nev, "radius": radius}
+    for name, prec, r in (("mixed_fresh", "mixed", 0.0), ("mixed_reuse", "mixed", radius),
+                          ("fp64_fresh", "fp64", 0.0), ("fp64_reuse", "fp64", radius)):
         lat, reused, warm, applies, resid = [], 0, 0, [], []
         with Server(workers=1, device=local) as srv:
             for k in range(steps):
-                res = srv.result(srv.submit_eigen(P, tau + k * spacing, nev, which, seed=900 + k,
+                res = srv.result(srv.submit_eigen(P, tau + k * spacing, nev, which, seed=900 + k, precision=prec,
                                                   reuse_radius=r, vectors=True))
                 lat.append(res["run_ms"])
                 st = res["stats"]
@@ -333,7 +334,8 @@ def tracking_bench(A, B, lay, local, tau, nev, which, steps=10, spacing=0.004j, 
         out[name] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                      "mean_ms": float(np.mean(lat)), "factor_reused": reused, "warm_started": warm,
                      "op_applies_mean": float(np.mean(applies)), "max_eig_resid": max(resid)}
-    out["speedup_mean_latency"] = out["fresh"]["mean_ms"] / out["reuse"]["mean_ms"]
+    out["reuse_speedup_mean_latency"] = {p: out[p + "_fresh"]["mean_ms"] / out[p + "_reuse"]["mean_ms"]
+                                         for p in ("mixed", "fp64")}
     return out
 
 
@@ -845,6 +847,7 @@ def main():
                                        "ncu capture of the 120-block case, scaled by the block count",
                      "bytes_per_launch": prof["sweep_bytes"],
                      "avg_launch_ms": sweep_ms, "launches": prof["sweeps"],
+                     "ctas_per_sm": prof["sweep_ctas_per_sm"],
                      "sweep_share_of_step": prof["sweep_ms"] / total_ms,
                      "factor_ms_avg": prof["factor_ms"] / max(prof["factors"], 1),
                      "step_breakdown_ms": {k: prof[k] / args.steps for k in ("sweep_ms", "factor_ms", "spmv_ms",

@@ -113,8 +113,8 @@ typedef struct {
     int32_t warm;
     /* Batched and served eigensolves (kore_eigs_shifts, the serving queue): > 0 lets a target
      * run on an idle slot whose factorised shift lies within this distance of the target,
-     * as sigma of that slot, without re-factorising, and started warm.  0: only a slot
-     * holding exactly the target's shift is reused. */
+     * as sigma of that slot, without re-factorising.  0: only a slot holding exactly the
+     * target's shift is reused. */
     double  reuse_radius;
 } kore_eps_opts;
 
@@ -231,7 +231,8 @@ int kore_plan_stream(const kore_plan *plan, void **stream);
  * (and clears the totals), 0 stops.  out (may be NULL) receives 12 doubles:
  * [sweep kernel ms total, sweeps that ran, factorisation ms total, factorisations,
  *  algorithmic bytes of one sweep launch, algorithmic flops of one factorisation,
- *  sparse-product ms, count, orthogonalisation ms, count, projected-problem ms, count].
+ *  sparse-product ms, count, orthogonalisation ms, count, projected-problem ms, count,
+ *  CTAs per SM of the last sweep launch]: 13 doubles.
  */
 int kore_profile(kore_plan *plan, int enable, double *out);
 

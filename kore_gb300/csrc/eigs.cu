@@ -592,6 +592,27 @@ __global__ void k_sum_cols(int64_t np, const double2 *__restrict__ V, int n, dou
     }
 }
 
+// v <- v / ||v||_2 (one CTA; a zero vector is left as it is)
+__global__ void k_unit(int64_t np, double2 *__restrict__ v) {
+    double s = 0.0;
+    for (int64_t r = threadIdx.x; r < np; r += blockDim.x) s += abs2(v[r]);
+    s = warp_sum_d(s);
+    __shared__ double sm[32];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sm[q];
+    if (!(t > 0.0)) return;
+    const double inv = rsqrt(t);
+    for (int64_t r = threadIdx.x; r < np; r += blockDim.x) v[r] = inv * v[r];
+}
+
+// y <- y + x
+__global__ void k_add(int64_t np, const double2 *__restrict__ x, double2 *__restrict__ y) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < np; r += (int64_t)gridDim.x * blockDim.x)
+        y[r] = y[r] + x[r];
+}
+
 __global__ void k_copy_vecs(int64_t np, TVec src, TVec dst, unsigned mask) {
     const int tg = blockIdx.y;
     if (!in_mask(mask, tg)) return;
@@ -912,20 +933,27 @@ int start_target(Run &r, int s, const EigsTarget &t) {
     x.nout = 0; x.k = 0; x.pstep = 0;
     r.sb.m[s] = x.m; r.sb.which[s] = ot.which; r.sb.tre[s] = ot.target_re; r.sb.tim[s] = ot.target_im;
     r.sb.sre[s] = sh.x; r.sb.sim[s] = sh.y;
-    // start vector: the slot's warm vector, or seeded (original order) -> padded; then
-    // normalised into column 0
+    // start vector: seeded (original order) -> padded; warm: the seeded vector and the
+    // slot's warm vector, both of unit norm, added.  The warm vector alone would not do:
+    // it lies in the invariant subspace of the previous target's eigenvectors, where the
+    // Krylov space would stop, so the seeded part keeps the other directions in it.
+    // Then normalised into column 0.
     double2 *orig = c.xin + (int64_t)s * c.np, *pad = c.w + (int64_t)s * c.np;
-    std::vector<double2> hv;
-    if (ot.warm && s < (int)p->warm_ok.size() && p->warm_ok[s]) {
-        KORE_CUDA_TRY(cudaMemcpyAsync(pad, p->d_warm + (int64_t)s * c.np, c.np * sizeof(double2),
-                                      cudaMemcpyDeviceToDevice, p->stream));
+    std::vector<double2> hv((size_t)p->n);
+    start_vector(p->n, ot.seed, hv.data());
+    const bool warm = ot.warm && s < (int)p->warm_ok.size() && p->warm_ok[s];
+    if (warm) {
+        double nn = 0.0;
+        for (const double2 &e : hv) nn += e.x * e.x + e.y * e.y;
+        const double inv = nn > 0.0 ? 1.0 / std::sqrt(nn) : 1.0;
+        for (double2 &e : hv) { e.x *= inv; e.y *= inv; }
+    }
+    KORE_CUDA_TRY(cudaMemcpyAsync(orig, hv.data(), hv.size() * sizeof(double2), cudaMemcpyHostToDevice, p->stream));
+    KORE_TRY(kore_gather(p, orig, pad));
+    if (warm) {
+        k_add<<<c.grid, 256, 0, p->stream>>>(c.np, p->d_warm + (int64_t)s * c.np, pad);
+        KORE_LAUNCHED(1);
         x.tgt.warm_started = 1;
-    } else {
-        hv.resize((size_t)p->n);
-        start_vector(p->n, ot.seed, hv.data());
-        KORE_CUDA_TRY(cudaMemcpyAsync(orig, hv.data(), hv.size() * sizeof(double2), cudaMemcpyHostToDevice,
-                                      p->stream));
-        KORE_TRY(kore_gather(p, orig, pad));
     }
     TCols tc{};
     tc.mask = 1u << s;
@@ -963,7 +991,7 @@ int fill_slots(Run &r) {
             if (!r.sl[u].busy && r.sl[u].valid && r.p->sigmas[u].x == sh.x && r.p->sigmas[u].y == sh.y) s = u;
         if (s < 0 && t.opts.reuse_radius > 0.0 && !t.opts.has_shift) {
             // the idle slot whose factors lie nearest the target, within the radius: run
-            // there with that slot's shift, started from its last eigenvectors
+            // there with that slot's shift (started warm only if the target asks for it)
             double best = t.opts.reuse_radius;
             for (int u = 0; u < r.T; ++u)
                 if (!r.sl[u].busy && r.sl[u].valid) {
@@ -974,7 +1002,6 @@ int fill_slots(Run &r) {
                 t.opts.has_shift = 1;
                 t.opts.shift_re = r.p->sigmas[s].x;
                 t.opts.shift_im = r.p->sigmas[s].y;
-                t.opts.warm = 1;
             }
         }
         for (int u = 0; u < r.T && s < 0; ++u)
@@ -1049,7 +1076,8 @@ int finish_target(Run &r, int s) {
     // the slot's warm vector for a later target: the sum of the eigenvectors just returned
     if (x.nout > 0 && x.nconv > 0 && s < p->warm_cap) {
         k_sum_cols<<<c.grid, 256, 0, p->stream>>>(c.np, x.Vt, x.nout, p->d_warm + (int64_t)s * c.np);
-        KORE_LAUNCHED(1);
+        k_unit<<<1, 1024, 0, p->stream>>>(c.np, p->d_warm + (int64_t)s * c.np);
+        KORE_LAUNCHED(2);
         KORE_CUDA_TRY(cudaGetLastError());
         p->warm_ok[s] = 1;
     }

@@ -123,7 +123,10 @@ constexpr int kChunkBytes = 16384;
 constexpr int kTileRows = 32;
 constexpr int kMaxRing = 13;
 constexpr int kEllReg = 4;   // level-0 coupling entries per thread held in registers (width 32)
-constexpr int kFill = 4;     // input-vector loads in flight per consumer lane
+// input-vector loads in flight per consumer lane: a two-matrix tile's slice (2 x 7 x 16
+// entries per warp at S = 400) takes one round of L2 latency with 8, two with 4; the
+// variants whose register budget (65536 / (192 CPS)) cannot hold 8 keep 4
+template <typename C, int CPS> constexpr int fill_of() { return (CPS == 2 || (CPS == 3 && sizeof(C) == 8)) ? 8 : 4; }
 
 enum { kMapDinv = 0, kMapG = 1, kMapH = 2, kMapLU = 3 };
 
@@ -214,6 +217,7 @@ template <typename C, int CPS>
 __global__ void __launch_bounds__(kTmaThreads, CPS) k_sweep_tma(const __grid_constant__ SweepTmaParams P) {
     using Shape = TmaShape<C>;
     constexpr int kCols = Shape::kCols, kCpw = Shape::kColsPerWarp;
+    constexpr int kFill = fill_of<C, CPS>();
     const SweepArgs &a = P.a;
     const int nst = P.nst;
     extern __shared__ __align__(1024) unsigned char smem_raw[];

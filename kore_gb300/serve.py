@@ -61,14 +61,14 @@ class Server:
         return t.value
 
     def submit_eigen(self, data, target, nev, which="TM", tol=1e-15, maxit=50, ncv=0, precision="mixed", seed=1,
-                     vectors=False, key=None, refine_tol=0.0, reuse_radius=0.0):
+                     vectors=False, key=None, refine_tol=0.0, reuse_radius=0.0, warm=False):
         """Eigensolve of data's pencil around `target` (kore_eigs); returns a ticket.
 
         reuse_radius > 0: when an idle slot of the pencil's cached plan holds factors at a
         shift within this distance of the target, the request runs there with that shift
-        (no re-factorisation; eigenvalues still sorted from the target) and starts from the
-        eigenvectors that slot returned last.  Its result then depends on that earlier
-        request, within the solver's tolerance."""
+        (no re-factorisation; eigenvalues still sorted from the target).  warm: start from
+        the seeded vector plus the eigenvectors that slot returned last.  Either makes the
+        result depend on earlier requests, within the solver's tolerance."""
         target = complex(target)
         ncv_eff = ncv if ncv > 0 else L.default_ncv(data.n, nev)
         evals = np.zeros(ncv_eff, dtype=np.complex128)
@@ -83,7 +83,7 @@ class Server:
         r.sigma_re, r.sigma_im = target.real, target.imag
         r.opts = L.EpsOpts(nev=nev, ncv=ncv, tol=tol, maxit=maxit, which=L.WHICH[which], target_re=target.real,
                            target_im=target.imag, seed=seed, purify=1, refine_tol=refine_tol,
-                           reuse_radius=float(reuse_radius))
+                           reuse_radius=float(reuse_radius), warm=int(bool(warm)))
         r.evals = evals.ctypes.data
         r.evecs = evecs.ctypes.data if vectors else None
         r.max_pairs = ncv_eff

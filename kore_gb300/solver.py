@@ -151,11 +151,12 @@ class Pencil:
     def profile(self, enable):
         """Start (True) / stop (False) CUDA-event timing of the sweep and factorisation
         kernels; returns the totals recorded so far."""
-        out = np.zeros(12)
+        out = np.zeros(13)
         L.check(self.lib.kore_profile(self._plan, 1 if enable else 0, L.ptr(out)), "kore_profile")
         return {"sweep_ms": out[0], "sweeps": int(out[1]), "factor_ms": out[2], "factors": int(out[3]),
                 "sweep_bytes": out[4], "factor_flops": out[5], "spmv_ms": out[6], "spmv_n": int(out[7]),
-                "ortho_ms": out[8], "ortho_n": int(out[9]), "schur_ms": out[10], "schur_n": int(out[11])}
+                "ortho_ms": out[8], "ortho_n": int(out[9]), "schur_ms": out[10], "schur_n": int(out[11]),
+                "sweep_ctas_per_sm": int(out[12])}
 
     def device_bytes(self):
         v = C.c_int64()
@@ -211,7 +212,7 @@ def forced_sweep(pencil, omegas, b, precision="mixed", group=16, refine_tol=0.0,
 
 
 def eigs_targets(pencil, targets, nev, which="TM", precision="mixed", tol=1e-15, maxit=50, seeds=None, ncv=0,
-                 purify=True, refine_tol=0.0, vectors=True, slots=None, reuse_radius=0.0):
+                 purify=True, refine_tol=0.0, vectors=True, slots=None, reuse_radius=0.0, warm=False):
     """Shift-and-invert Krylov-Schur at several targets of one pencil, the targets
     stepping together in shared launches (``kore_eigs_shifts``).  ``slots`` targets run
     at a time (default: all); when one finishes, the next takes its slot (its shift is
@@ -226,8 +227,8 @@ def eigs_targets(pencil, targets, nev, which="TM", precision="mixed", tol=1e-15,
 
     ``reuse_radius`` > 0: a later target runs on an idle slot whose shift lies within this
     distance of it (that shift is the spectral transformation's, the eigenvalues are still
-    sorted from the target), without re-factorising, started from the eigenvectors the
-    slot returned last.
+    sorted from the target), without re-factorising.  ``warm``: a target starts from its
+    seeded vector plus the eigenvectors its slot returned last.
 
     Returns a list of (eigenvalues, eigenvectors or None, stats dict), one per target.
     """
@@ -245,7 +246,7 @@ def eigs_targets(pencil, targets, nev, which="TM", precision="mixed", tol=1e-15,
         mx = max(mx, m)
         opts[t] = L.EpsOpts(nev=k, ncv=int(ncv), tol=tol, maxit=maxit, which=L.WHICH[which], target_re=tg[t].real,
                             target_im=tg[t].imag, seed=int(sds[t]), purify=int(purify),
-                            refine_tol=refine_tol, reuse_radius=float(reuse_radius))
+                            refine_tol=refine_tol, reuse_radius=float(reuse_radius), warm=int(bool(warm)))
     ev = np.zeros((T, mx), dtype=np.complex128)
     X = np.zeros((T, mx, pencil.n), dtype=np.complex128) if vectors else None
     nconv = (C.c_int * T)()
