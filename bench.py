@@ -470,6 +470,10 @@ def forced_bench(args, local, c=None, emit=True):
 MAC = {
     "mac3": dict(m=1, symm=1, Ek=1e-6, N=200, lmax=200, ricb=0.35, Em=1e-3, Le2=1e-8, Prandtl=1.0,
                  tau=0.1j, nev=8, which="TM", log10_ra0=8.9),
+    # the same physics with 60 of the 100 l-superblocks and N=120: small case for profiler
+    # captures (factors of ~0.3 GB, above the L2 size)
+    "mac3s": dict(m=1, symm=1, Ek=1e-6, N=120, lmax=120, ricb=0.35, Em=1e-3, Le2=1e-8, Prandtl=1.0,
+                  tau=0.1j, nev=8, which="TM", log10_ra0=8.9),
 }
 
 
@@ -511,8 +515,13 @@ def mac_bench(args, local, c=None, emit=True):
     spec = (tau, nev, which)
     E64, lat64, pairs64, _ = time_arm(p, torch, stream, spec, "fp64", steps, 1, seed0=600)
     l0 = kernel_launches()
+    p.profile(True)
     E, lat, pairs, _ = time_arm(p, torch, stream, spec, "mixed", steps, 1, seed0=600)
+    prof = p.profile(False)
     launches = kernel_launches() - l0
+    hbm, _, src = peaks()
+    sweep_ms = prof["sweep_ms"] / max(prof["sweeps"], 1)
+    achieved = prof["sweep_bytes"] / (sweep_ms * 1e-3) / 1e9
     lam, X = E.eigenvalues(), E.eigenvectors()
     lam64, X64 = E64.eigenvalues(), E64.eigenvectors()
     res = rel_residuals(A, Bn, lam[:nev], X[:, :nev])
@@ -534,7 +543,12 @@ def mac_bench(args, local, c=None, emit=True):
            "factor_s": E.stats.get("factor_s"),
            "solver_stats": {k: E.stats.get(k) for k in ("restarts", "op_applies", "sweeps", "refine_iters_max")},
            "max_rel_eig_diff_vs_fp64": float(dists.max()), "eigs_matching_fp64_1e-10": int((dists < 1e-10).sum()),
-           "gpu_launches": int(launches)}
+           "gpu_launches": int(launches),
+           "roofline": {"bound": "hbm", "kernel": "k_sweep_tma", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                        "frac": achieved / hbm, "peak_source": src, "bytes_per_launch": prof["sweep_bytes"],
+                        "avg_launch_ms": sweep_ms, "ctas_per_sm": prof["sweep_ctas_per_sm"],
+                        "step_breakdown_ms": {k: prof[k] / len(lat) for k in ("sweep_ms", "factor_ms", "spmv_ms",
+                                                                             "ortho_ms", "schur_ms")}}}
     if not args.no_parity:
         out["parity"] = parity_block(A, Bn, lay, tau, nev, lam, X, None)
     p.close()
