@@ -678,7 +678,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="leave the serving summary out")
     ap.add_argument("--no-mac", action="store_true", help="leave the dipole MAC summary out")
     ap.add_argument("--no-track", action="store_true", help="leave the target-tracking serving summary out")
-    ap.add_argument("--batch", type=int, default=4, help="targets of the batched form (1: skip it)")
+    ap.add_argument("--batch", type=int, default=8, help="targets of the batched form (1: skip it)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -601,9 +601,9 @@ int kore_plan_estimate_bytes(const kore_pencil_desc *d, int precision, int nshif
     }
     b += c * (3 * np * 16 + 2 * (np / 64 + np / 8 + 1024) * 8 + (nlev > 0 ? 3 * nlev + 2 : 1) * K * 4 + ell * e + 128);
     b += 2 * d->n * c * 16;   // kore_solve's device copies of b and x
-    // per target (one per shift): Krylov basis, its restart copy, a gathered input vector
-    // and the projected-problem workspace
-    if (ncv > 0) b += c * (2 * np * (int64_t)(ncv + 1) * 16 + np * 16 + (int64_t)(65 * 64 * 4 + 8 * 65 + 2048 * 65 + 4096) * 16);
+    // per target (one per shift): Krylov basis, its restart copy, a gathered input vector,
+    // the slot's warm-start vector and the projected-problem workspace
+    if (ncv > 0) b += c * (2 * np * (int64_t)(ncv + 1) * 16 + 2 * np * 16 + (int64_t)(65 * 64 * 4 + 8 * 65 + 2048 * 65 + 4096) * 16);
     b += 128LL << 20;   // allocation granularity of ~50 buffers
     *bytes = b;
     return KORE_OK;
