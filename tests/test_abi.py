@@ -75,3 +75,15 @@ def test_batch_api_rejects_bad_arguments():
     st = ctypes.c_int()
     assert lib.kore_batch_poll(None, 1, 0, ctypes.byref(st)) == 1
     assert lib.kore_batch_destroy(None) == 0
+
+
+def test_default_basis_size_rule():
+    """The eigensolver's basis when none is given (include/kore_gpu.h, kore_eps_opts.ncv
+    = 0): SLEPc's max(2 nev, nev + 15), raised to 4 nev up to 64, never above n."""
+    from kore_gb300._lib import MAX_NCV, default_ncv
+    assert MAX_NCV == 64
+    assert default_ncv(240000, 16) == 64      # the headline solve
+    assert default_ncv(240000, 8) == 32       # config 3: 4 nev
+    assert default_ncv(240000, 4) == 19       # SLEPc's nev + 15 dominates
+    assert default_ncv(240000, 40) == 80      # SLEPc's 2 nev above the cap (refused by the engine)
+    assert default_ncv(30, 16) == 30          # never above n
