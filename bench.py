@@ -127,9 +127,33 @@ def build_pencil(w):
     from kore_gb300.assembly import hydro_params, hydro_pencil
     from kore_gb300.structure import layout_from_params
     m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[w]
+    t0 = time.perf_counter()
     A, B = hydro_pencil(m, symm, Ek, N, lmax, ricb)
+    ASSEMBLY["host_s"] = time.perf_counter() - t0
     lay = layout_from_params(hydro_params(m, symm, Ek, N, lmax, ricb))
     return A, B, lay
+
+
+ASSEMBLY = {}
+
+
+def assembly_bench(w, A, B, device, reps=2):
+    """The pencil assembled on the GPU (kore_assemble_blocks) against the host assembly:
+    wall time of each (radial operators, patterns, values, the copy back) and the
+    relative Frobenius difference of the two results."""
+    import scipy.sparse.linalg as ssl
+    from kore_gb300.assembly import hydro_pencil
+    m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[w]
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        Ad, Bd = hydro_pencil(m, symm, Ek, N, lmax, ricb, assemble_on_device=True, device=device)
+        ts.append(time.perf_counter() - t0)
+    out = {"host_s": ASSEMBLY.get("host_s"), "device_s": min(ts), "device_gpu": device,
+           "rel_diff_A": float(ssl.norm(Ad - A) / ssl.norm(A)), "rel_diff_B": float(ssl.norm(Bd - B) / ssl.norm(B)),
+           "nnz": int(Ad.nnz + Bd.nnz)}
+    out["speedup"] = out["host_s"] / out["device_s"] if out["host_s"] else None
+    return out
 
 
 def run_eps(p, tau, nev, which, precision, seed, want_vectors=True, tol=1e-15, maxit=50):
@@ -678,6 +702,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="leave the serving summary out")
     ap.add_argument("--no-mac", action="store_true", help="leave the dipole MAC summary out")
     ap.add_argument("--no-track", action="store_true", help="leave the target-tracking serving summary out")
+    ap.add_argument("--no-asm", action="store_true", help="leave the GPU assembly timing out")
     ap.add_argument("--batch", type=int, default=8, help="targets of the batched form (1: skip it)")
     args = ap.parse_args()
 
@@ -712,6 +737,7 @@ def main():
     kb.build()
     m, symm, Ek, N, lmax, ricb, tau, nev, which = WORKLOADS[args.workload]
     A, B, lay = build_pencil(args.workload)
+    asm = None if args.no_asm or local != 0 else assembly_bench(args.workload, A, B, local)
 
     # ---- device-resident arms (pencil uploaded once, outside the timed region)
     p = Pencil(A, B, layout=lay, device=local)
@@ -874,6 +900,7 @@ def main():
         "serving": serve and {k: serve[k] for k in ("metric", "value", "unit", "config", "rates")},
         "mac_dipole": mac,
         "serving_tracking": track,
+        "assembly": asm,
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)

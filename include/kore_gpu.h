@@ -343,6 +343,28 @@ int kore_gegenbauer_mult(int device, int N, const double *a0, double lam, int h,
  * runs over the degrees in a process pool; the sums over degrees, the scaling by
  * OmgTau Ek and the power-balance residuals are kore_gb300.diagnostics'.
  */
+/*
+ * Values and column indices of a block-structured pencil matrix assembled on the GPU
+ * (bin/assemble.py:606-1176: A and B from the radial operators of bin/submatrices.py).
+ * Unknowns in nrowblk blocks of n1.  ops: nops dense n1 x n1 complex radial operators,
+ * row-major.  Block (R, C) of the matrix is sum_e coef_e op_e over the entries
+ * e in [ent_ptr[R], ent_ptr[R+1]) with ent_col[e] = C (ent_op, ent_coef complex), except
+ * that the first bc_g[R] rows of block R are its boundary rows, bc_vals + bc_ptr[R]
+ * (bc_g[R] x n1 complex, row-major, in the columns of block R).  The sparsity pattern is
+ * given per signature: row block R uses signature sig_of[R], whose local row i has the
+ * entries sig_pat[sig_rowptr[s (n1+1) + i] .. sig_rowptr[s (n1+1) + i + 1]) as pairs
+ * (block offset dC, local column j), column (R + dC) n1 + j, in increasing column order.
+ * indptr (nrows + 1 = nrowblk n1 + 1, host) must hold the row lengths those patterns
+ * give; indices (int32) and values (complex) receive the nnz entries (host arrays).
+ * Synchronous; every array is checked against the others before the device is touched.
+ */
+int kore_assemble_blocks(int device, int n1, int nops, const double *ops, int64_t nrowblk,
+                         const int32_t *sig_of, int nsig, const int32_t *sig_rowptr, int64_t npat,
+                         const int32_t *sig_pat, const int64_t *ent_ptr, const int32_t *ent_col,
+                         const int32_t *ent_op, const double *ent_coef, const int32_t *bc_g,
+                         const int64_t *bc_ptr, int64_t bc_len, const double *bc_vals,
+                         const int64_t *indptr, int64_t nnz, int32_t *indices, double *values);
+
 int kore_flow_diagnostics(int device, int N, double ricb, int npol, const int32_t *lpol, int ntor,
                           const int32_t *ltor, const double *x, int nvec, double *out);
 

@@ -25,6 +25,7 @@ Olver & Townsend (SIAM Review 55, 2013): a closed-form first coefficient followe
 a three-term ratio recurrence, evaluated here for all (row, column) pairs of the
 band at once.
 """
+import contextlib
 import math
 
 import numpy as np
@@ -286,24 +287,193 @@ def boundary_values(x, N, nder, ricb, rcmb=RCMB):
     return out
 
 
+# Inside ``lazy_blocks()`` kron_sum and bc_block return LazyBlock term lists instead of
+# sparse matrices, for assemble_grid to assemble on the GPU (one thread at a time).
+_LAZY = [False]
+
+
+@contextlib.contextmanager
+def lazy_blocks():
+    """Build the blocks of the pencil as term lists (LazyBlock) for ``assemble_grid``."""
+    _LAZY[0] = True
+    try:
+        yield
+    finally:
+        _LAZY[0] = False
+
+
+class LazyBlock:
+    """A block of the section grid (nrow x ncol l-blocks of n1 unknowns) kept as its terms:
+    (ks, js, vals, M) puts vals[t] * M at block (ks[t], js[t]); ``bc`` = (g, rows) puts
+    rows[k] (g x n1) in the first g rows of diagonal block k.  Supports the scalar
+    products, sums and differences the assembly uses."""
+
+    def __init__(self, nrow, ncol, terms=(), bc=None):
+        self.nrow, self.ncol = nrow, ncol
+        self.terms = list(terms)
+        self.bc = bc
+
+    def __mul__(self, a):
+        a = complex(a)
+        return LazyBlock(self.nrow, self.ncol, [(ks, js, a * v, M) for ks, js, v, M in self.terms],
+                         None if self.bc is None else (self.bc[0], a * self.bc[1]))
+
+    __rmul__ = __mul__
+
+    def __neg__(self):
+        return self * -1.0
+
+    def __add__(self, o):
+        if o is None:
+            return self
+        if (o.nrow, o.ncol) != (self.nrow, self.ncol) or (self.bc is not None and o.bc is not None):
+            raise ValueError("incompatible lazy blocks")
+        return LazyBlock(self.nrow, self.ncol, self.terms + o.terms, self.bc if o.bc is None else o.bc)
+
+    __radd__ = __add__
+
+    def __sub__(self, o):
+        return self + (-o)
+
+
 def kron_sum(lrow, lcol, terms):
     """Sum over terms (d, coef, M) of kron(P, M), where P[k, j] = coef(l_k) for the blocks
     k of degree l_k = lrow[k] and j of degree lcol[j] = l_k + d: the coupling of degree l
     to degree l + d in the l-block layout of two sections.  ``coef`` takes an array of
-    degrees.  None if no block couples."""
+    degrees.  None if no block couples (a LazyBlock inside ``lazy_blocks()``)."""
     lrow = np.asarray(lrow)
     lcol = np.asarray(lcol)
     pos = {int(l): j for j, l in enumerate(lcol)}
-    out = None
+    out = LazyBlock(lrow.size, lcol.size) if _LAZY[0] else None
     for d, coef, M in terms:
         ks = np.array([k for k, l in enumerate(lrow) if int(l) + d in pos], dtype=np.int64)
         if ks.size == 0:
             continue
         js = np.array([pos[int(lrow[k]) + d] for k in ks], dtype=np.int64)
         vals = np.asarray(coef(lrow[ks].astype(float)), dtype=complex) * np.ones(ks.size)
+        if _LAZY[0]:
+            out.terms.append((ks, js, vals, M))
+            continue
         P = ss.csr_matrix((vals, (ks, js)), shape=(lrow.size, lcol.size))
         t = ss.kron(P, M, format="csr")
         out = t if out is None else out + t
+    return out
+
+
+def grid_arrays(grid, n1):
+    """The arrays ``kore_assemble_blocks`` takes for a grid of LazyBlock (or None) cells,
+    sections of l-blocks of n1 unknowns: the dense operators, the entries (row block,
+    column block, operator, coefficient) sorted by row block, the boundary rows, the row
+    patterns of the distinct block signatures (the (block offset, operator) pairs and
+    boundary rows of a row block) and the CSR row pointer."""
+    nsec_r, nsec_c = len(grid), len(grid[0])
+    nrow_sec = [next(c.nrow for c in row if c is not None) for row in grid]
+    ncol_sec = [next(grid[a][b].ncol for a in range(nsec_r) if grid[a][b] is not None) for b in range(nsec_c)]
+    ro = np.concatenate([[0], np.cumsum(nrow_sec)])
+    co = np.concatenate([[0], np.cumsum(ncol_sec)])
+    nblk = int(ro[-1])
+    if int(co[-1]) != nblk:
+        raise ValueError("assemble_grid builds square matrices")
+    ops, op_id = [], {}
+    R_l, C_l, O_l, V_l = [], [], [], []
+    bc_g = np.zeros(nblk, dtype=np.int32)
+    bc_rows = [None] * nblk
+    for a in range(nsec_r):
+        for b in range(nsec_c):
+            cell = grid[a][b]
+            if cell is None:
+                continue
+            for ks, js, vals, M in cell.terms:
+                if id(M) not in op_id:
+                    op_id[id(M)] = len(ops)
+                    ops.append(M)
+                R_l.append(ro[a] + ks)
+                C_l.append(co[b] + js)
+                O_l.append(np.full(ks.size, op_id[id(M)], dtype=np.int32))
+                V_l.append(vals)
+            if cell.bc is not None:
+                if ro[a] != co[b]:
+                    raise ValueError("boundary rows belong to diagonal blocks")
+                g, rows = cell.bc
+                for k in range(cell.nrow):
+                    bc_g[ro[a] + k] = g
+                    bc_rows[ro[a] + k] = rows[k]
+    R = np.concatenate(R_l).astype(np.int64)
+    order = np.argsort(R, kind="stable")
+    R = R[order]
+    ent_col = np.concatenate(C_l).astype(np.int32)[order]
+    ent_op = np.concatenate(O_l)[order]
+    ent_coef = np.ascontiguousarray(np.concatenate(V_l).astype(np.complex128)[order])
+    ent_ptr = np.concatenate([[0], np.cumsum(np.bincount(R, minlength=nblk))]).astype(np.int64)
+    # the operators' row patterns and dense copies
+    dense = np.zeros((len(ops), n1, n1), dtype=np.complex128)
+    pat = []
+    for q, M in enumerate(ops):
+        Mc = ss.csr_matrix(M)
+        dense[q] = Mc.toarray()
+        rr = np.repeat(np.arange(n1), np.diff(Mc.indptr))
+        pat.append((rr, Mc.indices.astype(np.int64)))
+    # signatures: the (block offset, operator) pairs and boundary rows of a row block
+    sig_of = np.zeros(nblk, dtype=np.int32)
+    sigs, keys = [], {}
+    for Rb in range(nblk):
+        e0, e1 = ent_ptr[Rb], ent_ptr[Rb + 1]
+        key = (tuple(sorted(set(zip((ent_col[e0:e1] - Rb).tolist(), ent_op[e0:e1].tolist())))), int(bc_g[Rb]))
+        if key not in keys:
+            keys[key] = len(sigs)
+            sigs.append(key)
+        sig_of[Rb] = keys[key]
+    sig_rowptr = np.zeros((len(sigs), n1 + 1), dtype=np.int32)
+    pats, rowlen, base = [], np.zeros((len(sigs), n1), dtype=np.int64), 0
+    for s, (pairs, g) in enumerate(sigs):
+        ii, dd, jj = [], [], []
+        for dC, q in pairs:
+            rr, cc = pat[q]
+            keep = rr >= g
+            ii.append(rr[keep]); dd.append(np.full(int(keep.sum()), dC)); jj.append(cc[keep])
+        if g > 0:
+            ii.append(np.repeat(np.arange(g), n1)); dd.append(np.zeros(g * n1, dtype=np.int64))
+            jj.append(np.tile(np.arange(n1), g))
+        ii, dd, jj = (np.concatenate(x).astype(np.int64) for x in (ii, dd, jj))
+        u = np.unique(np.stack([ii, dd, jj], axis=1), axis=0)   # sorted by row, then (dC, j)
+        rowlen[s] = np.bincount(u[:, 0], minlength=n1)
+        sig_rowptr[s] = base + np.concatenate([[0], np.cumsum(rowlen[s])])
+        pats.append(u[:, 1:].astype(np.int32))
+        base += len(u)
+    sig_pat = np.ascontiguousarray(np.concatenate(pats)) if pats else np.zeros((0, 2), np.int32)
+    indptr = np.concatenate([[0], np.cumsum(rowlen[sig_of].ravel())]).astype(np.int64)
+    nnz = int(indptr[-1])
+    bc_ptr = np.full(nblk, -1, dtype=np.int64)
+    chunks, off = [], 0
+    for Rb in range(nblk):
+        if bc_g[Rb] > 0:
+            bc_ptr[Rb] = off
+            chunks.append(np.asarray(bc_rows[Rb], dtype=np.complex128).reshape(-1))
+            off += chunks[-1].size
+    bc_vals = np.ascontiguousarray(np.concatenate(chunks)) if chunks else np.zeros(1, np.complex128)
+    return dict(n1=int(n1), nblk=nblk, ops=np.ascontiguousarray(dense), sig_of=sig_of,
+                sig_rowptr=np.ascontiguousarray(sig_rowptr), sig_pat=sig_pat, ent_ptr=ent_ptr,
+                ent_col=np.ascontiguousarray(ent_col), ent_op=np.ascontiguousarray(ent_op), ent_coef=ent_coef,
+                bc_g=bc_g, bc_ptr=bc_ptr, bc_len=int(off), bc_vals=bc_vals, indptr=indptr, nnz=nnz)
+
+
+def assemble_grid(grid, n1, device=0):
+    """CSR matrix of a grid of LazyBlock (or None) cells, sections of l-blocks of n1
+    unknowns, assembled on the GPU (``kore_assemble_blocks``): the row patterns are formed
+    here once per distinct block signature (``grid_arrays``), the values and column indices
+    of every row on the device.  Explicit zeros are removed, as in the host assembly."""
+    from . import _lib as L
+    g = grid_arrays(grid, n1)
+    indices = np.zeros(g["nnz"], dtype=np.int32)
+    values = np.zeros(g["nnz"], dtype=np.complex128)
+    L.check(L.load().kore_assemble_blocks(
+        int(device), g["n1"], len(g["ops"]), L.ptr(g["ops"]), g["nblk"], L.ptr(g["sig_of"]), len(g["sig_rowptr"]),
+        L.ptr(g["sig_rowptr"]), len(g["sig_pat"]), L.ptr(g["sig_pat"]), L.ptr(g["ent_ptr"]), L.ptr(g["ent_col"]),
+        L.ptr(g["ent_op"]), L.ptr(g["ent_coef"]), L.ptr(g["bc_g"]), L.ptr(g["bc_ptr"]), g["bc_len"],
+        L.ptr(g["bc_vals"]), L.ptr(g["indptr"]), g["nnz"], L.ptr(indices), L.ptr(values)), "kore_assemble_blocks")
+    n = g["nblk"] * g["n1"]
+    out = ss.csr_matrix((values, indices, g["indptr"]), shape=(n, n))
+    out.eliminate_zeros()
     return out
 
 
@@ -352,7 +522,10 @@ def momentum_blocks(op, m, lp, lt, visc, wf, Gaspard=1.0, pu=0, pv=0):
 
 def bc_block(rows_list, nrow, N1):
     """Block-diagonal matrix holding, for each l-block k, the boundary rows rows_list[k]
-    (nrow rows of N1 Chebyshev coefficients) in its first nrow rows."""
+    (nrow rows of N1 Chebyshev coefficients) in its first nrow rows (a LazyBlock inside
+    ``lazy_blocks()``)."""
+    if _LAZY[0]:
+        return LazyBlock(len(rows_list), len(rows_list), bc=(nrow, np.stack([np.asarray(r)[:nrow] for r in rows_list])))
     data, ri, ci = [], [], []
     for k, rows in enumerate(rows_list):
         for q in range(nrow):
@@ -393,7 +566,7 @@ def velocity_bc_blocks(lp, lt, N, ricb, bci=1, bco=1, forcing=0):
 
 def hydro_pencil(m, symm, Ek, N, lmax, ricb=0.35, bci=1, bco=1, forcing=0, forcing_frequency=0.0,
                  forcing_amplitude_cmb=1.0, forcing_amplitude_icb=0.0, Gaspard=1.0, ViscosD=None,
-                 with_norm=False, device=None):
+                 with_norm=False, device=None, assemble_on_device=False):
     """(A, B) as bin/assemble.py writes them for the hydrodynamic shell problem.
 
     forcing == 0: eigenproblem, B is the (sizmat x sizmat) float64 matrix, A and B
@@ -401,7 +574,10 @@ def hydro_pencil(m, symm, Ek, N, lmax, ricb=0.35, bci=1, bco=1, forcing=0, forci
     forced problem, A = i w u + Coriolis - viscous (unnormalised) and B is the
     (sizmat x 1) forcing column.  The forced matrix at frequency w is therefore
     ||B||_F (A_eig - i w B_eig) of the eigen pencil.  ``device``: build the Gegenbauer
-    multiplication operators on that GPU instead of the host.
+    multiplication operators on that GPU instead of the host.  ``assemble_on_device``:
+    assemble A and B from the radial operators on the GPU (``device``, else GPU 0) with
+    ``assemble_grid``; the host then forms only the row patterns of the distinct block
+    signatures.
     """
     if ricb <= 0:
         raise ValueError("only the spherical shell (ricb > 0) is assembled here")
@@ -411,12 +587,20 @@ def hydro_pencil(m, symm, Ek, N, lmax, ricb=0.35, bci=1, bco=1, forcing=0, forci
     lp, lt = ell(m, lmax, symm)
     wf = forcing_frequency if forcing else 0.0
     R = RadialOperators(N, ricb, device=device)
-    App, Apt, Atp, Att, u_p, u_t = momentum_blocks(R.op, m, lp, lt, visc, wf, Gaspard)
-    BCp, BCt = velocity_bc_blocks(lp, lt, N, ricb, bci, bco, forcing)
-    A = ss.bmat([[App + BCp, Apt], [Atp, Att + BCt]], format="csr").astype(np.complex128)
-    A.eliminate_zeros()
+    with lazy_blocks() if assemble_on_device else contextlib.nullcontext():
+        App, Apt, Atp, Att, u_p, u_t = momentum_blocks(R.op, m, lp, lt, visc, wf, Gaspard)
+        BCp, BCt = velocity_bc_blocks(lp, lt, N, ricb, bci, bco, forcing)
+    gpu = 0 if device is None else device
+    if assemble_on_device:
+        A = assemble_grid([[App + BCp, Apt], [Atp, Att + BCt]], N, gpu)
+    else:
+        A = ss.bmat([[App + BCp, Apt], [Atp, Att + BCt]], format="csr").astype(np.complex128)
+        A.eliminate_zeros()
     if forcing == 0:
-        B = ss.bmat([[-u_p, None], [None, -u_t]], format="csr").real.astype(np.float64)
+        if assemble_on_device:
+            B = assemble_grid([[-u_p, None], [None, -u_t]], N, gpu).real.astype(np.float64)
+        else:
+            B = ss.bmat([[-u_p, None], [None, -u_t]], format="csr").real.astype(np.float64)
         B.eliminate_zeros()
         bnorm = ss.linalg.norm(B)
         if with_norm:

@@ -30,11 +30,13 @@ The field enters through the Chebyshev coefficients of r^X h^(J)(r), h = r^-2 / 
 dipole's poloidal scalar, scaled to unit magnetic energy (``dipole_norm``).  Only the
 eigenproblem (no forcing) is assembled.
 """
+import contextlib
+
 import numpy as np
 import scipy.sparse as ss
 
-from .assembly import (RCMB, RadialOperators, bc_block, boundary_values, dipole_norm, kron_sum,
-                       momentum_blocks, velocity_bc_blocks)
+from .assembly import (RCMB, RadialOperators, assemble_grid, bc_block, boundary_values, dipole_norm, kron_sum,
+                       lazy_blocks, momentum_blocks, velocity_bc_blocks)
 from .structure import ell
 
 __all__ = ["mac_pencil", "mac_pencil_parts", "mac_params"]
@@ -105,10 +107,12 @@ def _induction(op, m, lp, lt, lmag_p, lmag_t):
 
 def mac_pencil_parts(m, symm, Ek, N, lmax, ricb=0.35, Em=None, Le2=None, Prandtl=1.0, cnorm="mag_energy",
                      heating="differential", bci=1, bco=1, bci_thermal=0, bco_thermal=0, Gaspard=1.0,
-                     device=None):
+                     device=None, assemble_on_device=False):
     """(A0, Ab, B, bnorm): the unnormalised eigen pencil with A = A0 + BV2 Ab, where
     BV2 = -Ra Ek^2 / Prandtl is the buoyancy factor (``bin/parameters.py:175-186``), so
-    that A is affine in the Rayleigh number; B does not depend on it."""
+    that A is affine in the Rayleigh number; B does not depend on it.
+    ``assemble_on_device``: A0 and B assembled on the GPU (``device``, else GPU 0) from the
+    radial operators (``assemble_grid``); Ab, one operator per block, stays on the host."""
     if ricb <= 0:
         raise ValueError("the dipole field needs an inner core (ricb > 0)")
     if (lmax - m + 1) % 2:
@@ -126,6 +130,30 @@ def mac_pencil_parts(m, symm, Ek, N, lmax, ricb=0.35, Em=None, Le2=None, Prandtl
     L = lambda l: l * (l + 1)
     nb = lp.size
 
+    with lazy_blocks() if assemble_on_device else contextlib.nullcontext():
+        A0g, Bg = _mac_blocks(op, mf, L, N, N1, ricb, Ek, Em, Le2, Prandtl, heating, bci, bco, bci_thermal,
+                              bco_thermal, Gaspard, lp, lt, lmag_p, lmag_t)
+    if assemble_on_device:
+        gpu = 0 if device is None else device
+        A0 = assemble_grid(A0g, N1, gpu)
+        B = assemble_grid(Bg, N1, gpu).real.astype(np.float64)
+    else:
+        A0 = ss.bmat(A0g, format="csr").astype(np.complex128)
+        A0.eliminate_zeros()
+        B = ss.block_diag([Bg[k][k] for k in range(5)], format="csr").real.astype(np.float64)
+    B.eliminate_zeros()
+    Ubuoy = kron_sum(lp, lp, [(0, L, op(6, 0, "u"))])   # L r^6 theta in section u
+    n = nb * N1
+    Ub = Ubuoy.tocoo()
+    Ab = ss.csr_matrix((Ub.data, (Ub.row, Ub.col + 4 * n)), shape=A0.shape, dtype=np.complex128)
+    Ab.eliminate_zeros()
+    return A0, Ab, B, float(ss.linalg.norm(B))
+
+
+def _mac_blocks(op, mf, L, N, N1, ricb, Ek, Em, Le2, Prandtl, heating, bci, bco, bci_thermal, bco_thermal,
+                Gaspard, lp, lt, lmag_p, lmag_t):
+    """The 5 x 5 section grid of A0 and the block diagonal of B (sparse blocks, or
+    LazyBlock term lists inside ``lazy_blocks()``)."""
     App, Apt, Atp, Att, Up, Ut = momentum_blocks(op, mf, lp, lt, Ek, 0.0, Gaspard, pu=2, pv=3)
     BCp, BCt = velocity_bc_blocks(lp, lt, N, ricb, bci, bco)
     u_bpol, u_btor = _lorentz_u(op, mf, lmag_p, lmag_t, lp)
@@ -152,7 +180,6 @@ def mac_pencil_parts(m, symm, Ek, N, lmax, ricb=0.35, Em=None, Le2=None, Prandtl
         Hu = kron_sum(lp, lp, [(0, L, op(2, 0, "h"))])
         Dh = kron_sum(lp, lp, [(0, lambda l: -L(l), op(0, 0, "h")), (0, lambda l: 2 + 0 * l, op(1, 1, "h")),
                                (0, lambda l: 1 + 0 * l, op(2, 2, "h"))])
-    Ubuoy = kron_sum(lp, lp, [(0, L, op(6, 0, "u"))])   # L r^6 theta in section u
 
     # boundary rows: insulating magnetic boundaries (inner on the first row), thermal
     Ta = boundary_values(-1, N, 4, ricb)
@@ -175,20 +202,14 @@ def mac_pencil_parts(m, symm, Ek, N, lmax, ricb=0.35, Em=None, Le2=None, Prandtl
     BCh = bc_block([rh for _ in lp], 2, N1)
 
     thermaD = Ek / Prandtl
-    A0 = ss.bmat([
-        [App + BCp, Apt, Le2 * u_bpol, Le2 * u_btor, None],
-        [Atp, Att + BCt, Le2 * v_bpol, Le2 * v_btor, None],
-        [f_up, f_ut, -Em * Df + BCf, None, None],
-        [g_up, g_ut, None, -Em * Dg + BCg, None],
-        [Hu, None, None, None, thermaD * Dh + BCh]], format="csr").astype(np.complex128)
-    A0.eliminate_zeros()
-    n = nb * N1
-    Ub = Ubuoy.tocoo()
-    Ab = ss.csr_matrix((Ub.data, (Ub.row, Ub.col + 4 * n)), shape=A0.shape, dtype=np.complex128)
-    Ab.eliminate_zeros()
-    B = ss.block_diag([-Up, -Ut, -Bf, -Bg, Th], format="csr").real.astype(np.float64)
-    B.eliminate_zeros()
-    return A0, Ab, B, float(ss.linalg.norm(B))
+    A0 = [[App + BCp, Apt, Le2 * u_bpol, Le2 * u_btor, None],
+          [Atp, Att + BCt, Le2 * v_bpol, Le2 * v_btor, None],
+          [f_up, f_ut, -Em * Df + BCf, None, None],
+          [g_up, g_ut, None, -Em * Dg + BCg, None],
+          [Hu, None, None, None, thermaD * Dh + BCh]]
+    diag = [-Up, -Ut, -Bf, -Bg, Th]
+    B = [[diag[a] if a == b else None for b in range(5)] for a in range(5)]
+    return A0, B
 
 
 def mac_pencil(m, symm, Ek, N, lmax, ricb=0.35, Em=None, Le2=None, Prandtl=1.0, Ra=0.0, with_norm=False, **kw):

@@ -123,3 +123,83 @@ def test_fullsize_bench_pencil_matches_reference_fingerprint():
     assert np.allclose(f["A_row1"], z["A_row1"], rtol=1e-13, atol=0)
     # explicit zeros aside, the sparsity matches
     assert abs(int(f["A_nnz"]) - int(z["A_nnz"])) <= 0.001 * int(z["A_nnz"])
+
+
+def _emulate_assemble_kernel(g):
+    """What kore_assemble_blocks computes, row by row in numpy: the column indices and
+    values of each row from its signature's pattern, the boundary rows and the entries."""
+    import scipy.sparse as ss
+    n1, nblk = g["n1"], g["nblk"]
+    indices = np.zeros(g["nnz"], dtype=np.int64)
+    values = np.zeros(g["nnz"], dtype=np.complex128)
+    for R in range(nblk):
+        rp = g["sig_rowptr"][g["sig_of"][R]]
+        e0, e1 = g["ent_ptr"][R], g["ent_ptr"][R + 1]
+        for i in range(n1):
+            pat = g["sig_pat"][rp[i]:rp[i + 1]]
+            C = R + pat[:, 0].astype(np.int64)
+            j = pat[:, 1].astype(np.int64)
+            if i < g["bc_g"][R]:
+                v = np.where(pat[:, 0] == 0, g["bc_vals"][g["bc_ptr"][R] + i * n1 + j], 0)
+            else:
+                v = np.zeros(len(pat), dtype=np.complex128)
+                for e in range(e0, e1):
+                    v = v + np.where(C == g["ent_col"][e], g["ent_coef"][e] * g["ops"][g["ent_op"][e], i, j], 0)
+            out = g["indptr"][R * n1 + i]
+            indices[out:out + len(pat)] = C * n1 + j
+            values[out:out + len(pat)] = v
+    n = nblk * n1
+    M = ss.csr_matrix((values, indices, g["indptr"]), shape=(n, n))
+    assert np.all(np.diff(indices[:g["indptr"][1]]) > 0)
+    M.eliminate_zeros()
+    return M
+
+
+@pytest.mark.parametrize("forcing", [0, 7])
+def test_device_assembly_inputs_rebuild_host_pencil(forcing):
+    """The lazy blocks and grid arrays that the GPU assembly takes rebuild the host
+    assembly's A and B: signatures, row patterns (sorted columns), boundary rows and
+    entry coefficients, checked through a numpy restatement of the kernel."""
+    import scipy.sparse as ss
+    from kore_gb300 import assembly as asm
+    m, symm, Ek, N, lmax, ricb = 2, 1, 1e-3, 24, 13, 0.35
+    lp, lt = asm.ell(m, lmax, symm)
+    R = asm.RadialOperators(N, ricb)
+    wf = 0.7 if forcing else 0.0
+    with asm.lazy_blocks():
+        App, Apt, Atp, Att, Up, Ut = asm.momentum_blocks(R.op, m, lp, lt, Ek, wf)
+        BCp, BCt = asm.velocity_bc_blocks(lp, lt, N, ricb, forcing=forcing)
+    gA = asm.grid_arrays([[App + BCp, Apt], [Atp, Att + BCt]], N)
+    assert len(gA["sig_rowptr"]) <= 8          # row blocks share a few signatures
+    A = _emulate_assemble_kernel(gA)
+    if forcing:
+        Ah, _ = asm.hydro_pencil(m, symm, Ek, N, lmax, ricb, forcing=forcing, forcing_frequency=wf)
+        assert ssl.norm(A - Ah) <= 1e-14 * ssl.norm(Ah)
+        return
+    B = _emulate_assemble_kernel(asm.grid_arrays([[-Up, None], [None, -Ut]], N)).real
+    Ah, Bh, nrm = asm.hydro_pencil(m, symm, Ek, N, lmax, ricb, with_norm=True)
+    assert ssl.norm(A / nrm - Ah) <= 1e-14 * ssl.norm(Ah)
+    assert ssl.norm(ss.csr_matrix(B) / nrm - Bh) <= 1e-14 * ssl.norm(Bh)
+    assert abs(ssl.norm(B) - nrm) <= 1e-14 * nrm
+
+
+def test_mac_device_assembly_inputs_rebuild_host_pencil():
+    """The same for the dipole MAC pencil's 5 x 5 section grid (Lorentz, induction and
+    heat blocks, insulating and thermal boundary rows)."""
+    import scipy.sparse as ss
+    from kore_gb300 import assembly as asm
+    from kore_gb300 import assembly_mac as mac
+    from kore_gb300.structure import ell
+    m, symm, Ek, N, lmax, ricb = 1, 1, 1e-3, 16, 8, 0.35
+    kw = dict(Em=0.1, Le2=1e-3, Prandtl=1.0)
+    A0h, _, Bh, nrm = mac.mac_pencil_parts(m, symm, Ek, N, lmax, ricb, **kw)
+    lp, lt = ell(m, lmax, symm)
+    lmag_p, lmag_t = ell(m, lmax, -symm)
+    R = asm.RadialOperators(N, ricb, field=asm.dipole_norm(ricb, "mag_energy"))
+    with asm.lazy_blocks():
+        A0g, Bg = mac._mac_blocks(R.op, float(m), lambda l: l * (l + 1), N, N, ricb, Ek, kw["Em"], kw["Le2"],
+                                  kw["Prandtl"], "differential", 1, 1, 0, 0, 1.0, lp, lt, lmag_p, lmag_t)
+    A0 = _emulate_assemble_kernel(asm.grid_arrays(A0g, N))
+    B = ss.csr_matrix(_emulate_assemble_kernel(asm.grid_arrays(Bg, N)).real)
+    assert ssl.norm(A0 - A0h) <= 1e-14 * ssl.norm(A0h)
+    assert ssl.norm(B - Bh) <= 1e-14 * ssl.norm(Bh)
