@@ -180,8 +180,9 @@ int kore_solve_dev(kore_plan *plan, const void *b_dev, void *x_dev, int nrhs,
  * complex128 device vectors in the original unknown order; the kernels run on
  * `stream` (0 = the legacy default stream) of the plan's device, and before returning
  * the call synchronises that stream and copies the scratch's error and NaN flags to
- * the host (KORE_ETIMEOUT, KORE_ENAN).  The first call on a device looks up the
- * scratch address (set-up); make that first call before any stream capture.  Every
+ * the host (KORE_ETIMEOUT, KORE_ENAN), so no call can be part of a stream capture
+ * (a call made while its stream captures invalidates the capture and returns
+ * KORE_ECUDA).  The first call on a device looks up the scratch address.  Every
  * call shares the one scratch array and keeps the last call's contents, so calls
  * whose work overlaps on the GPU (other threads, other streams) race: serialise them.
  */
