@@ -872,7 +872,9 @@ def main():
                   "solver_stats": {k: stats64.get(k) for k in ("restarts", "op_applies", "sweeps")}}
                  if lat64 else None),
         "speedup_vs_fp64": (value / (pairs64 / (sum(lat64) / 1e3))) if lat64 else None,
-        "batched": batched and {k: v for k, v in batched.items() if k != "results"},
+        "batched": batched and dict({k: v for k, v in batched.items() if k != "results"},
+                                    speedup_vs_fp64_single=(batched["value"] / (pairs64 / (sum(lat64) / 1e3))
+                                                            if lat64 else None)),
         "parity": parity,
         "max_eig_resid": float(res.max()), "max_rel_eig_diff_vs_fp64": diff,
         "eigs_matching_fp64_1e-10": nmatch, "max_rel_eig_diff_found_by_both": diff_both,
