@@ -571,6 +571,7 @@ def mac_bench(args, local, c=None, emit=True):
            "roofline": {"bound": "hbm", "kernel": "k_sweep_tma", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                         "frac": achieved / hbm, "peak_source": src, "bytes_per_launch": prof["sweep_bytes"],
                         "avg_launch_ms": sweep_ms, "ctas_per_sm": prof["sweep_ctas_per_sm"],
+                        "chunk_bytes": prof["sweep_chunk_bytes"],
                         "step_breakdown_ms": {k: prof[k] / len(lat) for k in ("sweep_ms", "factor_ms", "spmv_ms",
                                                                              "ortho_ms", "schur_ms")}}}
     if not args.no_parity:
@@ -889,7 +890,7 @@ def main():
                                        "ncu capture of the 120-block case, scaled by the block count",
                      "bytes_per_launch": prof["sweep_bytes"],
                      "avg_launch_ms": sweep_ms, "launches": prof["sweeps"],
-                     "ctas_per_sm": prof["sweep_ctas_per_sm"],
+                     "ctas_per_sm": prof["sweep_ctas_per_sm"], "chunk_bytes": prof["sweep_chunk_bytes"],
                      "sweep_share_of_step": prof["sweep_ms"] / total_ms,
                      "factor_ms_avg": prof["factor_ms"] / max(prof["factors"], 1),
                      "step_breakdown_ms": {k: prof[k] / args.steps for k in ("sweep_ms", "factor_ms", "spmv_ms",

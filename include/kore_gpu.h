@@ -229,11 +229,11 @@ int kore_plan_stream(const kore_plan *plan, void **stream);
 
 /*
  * Kernel timing with CUDA events on the plan's stream.  enable = 1 starts recording
- * (and clears the totals), 0 stops.  out (may be NULL) receives 12 doubles:
+ * (and clears the totals), 0 stops.  out (may be NULL) receives 14 doubles:
  * [sweep kernel ms total, sweeps that ran, factorisation ms total, factorisations,
  *  algorithmic bytes of one sweep launch, algorithmic flops of one factorisation,
  *  sparse-product ms, count, orthogonalisation ms, count, projected-problem ms, count,
- *  CTAs per SM of the last sweep launch]: 13 doubles.
+ *  CTAs per SM and ring chunk bytes of the last sweep launch].
  */
 int kore_profile(kore_plan *plan, int enable, double *out);
 

@@ -79,6 +79,7 @@ struct kore_plan {
     // on (all of them for kore_factor_shifts, one for a slot refill)
     int fw_lo = 0, fw_n = 0;
     int sweep_cps = 0;                // CTAs per SM of the last sweep (autotuned per plan shape)
+    int sweep_chunk = 0;              // its ring chunk bytes
     std::vector<double2> sigmas;      // host copy of the shifts
     std::vector<double> minfs;        // ||A - sigma_s B||_inf per shift
     double2 *d_sigma = nullptr;       // device copy of the shifts

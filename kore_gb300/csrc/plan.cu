@@ -538,6 +538,7 @@ int kore_profile(kore_plan *p, int enable, double *out) {
             out[7 + 2 * (k - 2)] = (double)p->prof_n[k];
         }
         out[12] = (double)p->sweep_cps;   // CTAs per SM of the last sweep (the autotuner's choice)
+        out[13] = (double)p->sweep_chunk;   // and its ring chunk bytes
     }
     if (enable) {
         for (int k = 0; k < 5; ++k) { p->prof_ms[k] = 0.0; p->prof_n[k] = 0; }

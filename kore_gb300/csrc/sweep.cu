@@ -112,16 +112,17 @@ __device__ __forceinline__ void wait_count(const int *c, int target, int *err) {
 // dozen entries per row) with plain coalesced loads instead.
 constexpr int kTmaConsumerWarps = 4;
 constexpr int kTmaConsumers = 32 * kTmaConsumerWarps;
-// CTAs per SM: with three CTAs of three or four 16 KB slots, ~200 KB per SM is in flight
-// and a CTA's per-tile work (input vectors, reduction, signalling) overlaps the other
-// CTAs' streaming.  Variants with 2 and 4 CTAs per SM are compiled too (deeper rings per
-// CTA, or more CTAs to overlap); the autotuner below picks one per plan shape.
-constexpr int kTmaCtasPerSm = 3;
-constexpr int kTmaVariants[] = {2, 3, 4};
+// Variants: 2, 3 or 4 CTAs per SM (deeper rings per CTA, or more CTAs whose per-tile
+// work -- input vectors, reduction, signalling -- overlaps the others' streaming) and
+// chunks of 8 or 16 KB (the ring holds the same bytes; with smaller chunks a consumed
+// chunk frees its slot sooner, so more of the ring is in flight).  The autotuner below
+// picks one per plan shape; untuned sweeps use 4 CTAs per SM and 8 KB chunks.
+struct TmaVariant { int cps, chunk; };
+constexpr TmaVariant kTmaVariants[] = {{2, 16384}, {3, 16384}, {4, 16384}, {2, 8192}, {3, 8192}, {4, 8192}};
+constexpr TmaVariant kTmaDefault = {4, 8192};
 constexpr int kTmaThreads = kTmaConsumers + 64;   // + one producer warp + one dependency-checker warp
-constexpr int kChunkBytes = 16384;
 constexpr int kTileRows = 32;
-constexpr int kMaxRing = 13;
+constexpr int kMaxRing = 24;
 constexpr int kEllReg = 4;   // level-0 coupling entries per thread held in registers (width 32)
 // input-vector loads in flight per consumer lane: a two-matrix tile's slice (2 x 7 x 16
 // entries per warp at S = 400) takes one round of L2 latency with 8, two with 4; the
@@ -136,8 +137,8 @@ struct SweepTmaParams {
     int nst;               // ring slots
 };
 
-template <typename C> struct TmaShape {
-    static constexpr int kCols = kChunkBytes / (kTileRows * (int)sizeof(C));   // columns per chunk
+template <typename C, int CHUNK> struct TmaShape {
+    static constexpr int kCols = CHUNK / (kTileRows * (int)sizeof(C));   // columns per chunk
     static constexpr int kColsPerWarp = kCols / kTmaConsumerWarps;
 };
 
@@ -213,9 +214,9 @@ __device__ __forceinline__ void decode_tile(int64_t g, int &k, const int64_t *st
     }
 }
 
-template <typename C, int CPS>
+template <typename C, int CPS, int CHUNK>
 __global__ void __launch_bounds__(kTmaThreads, CPS) k_sweep_tma(const __grid_constant__ SweepTmaParams P) {
-    using Shape = TmaShape<C>;
+    using Shape = TmaShape<C, CHUNK>;
     constexpr int kCols = Shape::kCols, kCpw = Shape::kColsPerWarp;
     constexpr int kFill = fill_of<C, CPS>();
     const SweepArgs &a = P.a;
@@ -225,7 +226,7 @@ __global__ void __launch_bounds__(kTmaThreads, CPS) k_sweep_tma(const __grid_con
     const int nc = (S + kCols - 1) / kCols;   // chunks per block
     const int nvec = nc * kCols;
     unsigned char *ring = smem_raw;
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)nst * kChunkBytes);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)nst * CHUNK);
     uint64_t *empty = full + nst;
     C *vbuf = reinterpret_cast<C *>(empty + nst);   // 2 x nvec input vectors (each warp fills its columns)
     __shared__ C red[2][kTmaConsumerWarps][33];   // per-warp partial sums, by tile parity
@@ -291,8 +292,8 @@ __global__ void __launch_bounds__(kTmaThreads, CPS) k_sweep_tma(const __grid_con
                     if (m >= t.nmat) break;
                     for (int ch = 0; ch < nc; ++ch) {
                         if (!mbar_wait(&empty[slot], ph ^ 1)) atomicCAS(a.err, 0, KORE_DEVERR_FLAG);
-                        mbar_arrive_expect_tx(&full[slot], kChunkBytes);
-                        tma_load_4d(ring + (size_t)slot * kChunkBytes, &P.maps[t.map[m]], &full[slot],
+                        mbar_arrive_expect_tx(&full[slot], CHUNK);
+                        tma_load_4d(ring + (size_t)slot * CHUNK, &P.maps[t.map[m]], &full[slot],
                                     2 * t.r0, ch * kCols, (int)t.mblk[m], (int)t.s);
                         ++issued;
                         if (++slot == (uint32_t)nst) { slot = 0; ph ^= 1; }
@@ -462,7 +463,7 @@ __global__ void __launch_bounds__(kTmaThreads, CPS) k_sweep_tma(const __grid_con
                     const C *vv = vbuf + m * nvec + w * kCpw;
                     for (int ch = 0; ch < nc; ++ch) {
                         if (!mbar_wait(&full[slot], ph)) atomicCAS(a.err, 0, KORE_DEVERR_FLAG);
-                        const C *bc = reinterpret_cast<const C *>(ring + (size_t)slot * kChunkBytes) +
+                        const C *bc = reinterpret_cast<const C *>(ring + (size_t)slot * CHUNK) +
                                       w * kCpw * kTileRows + lane;
                         const C *vc = vv + ch * kCols;
 #pragma unroll
@@ -725,10 +726,17 @@ __global__ void k_scatter(int64_t np, int64_t n, const int64_t *__restrict__ s2o
 
 
 template <typename C>
-size_t tma_smem(int S, int nst) {
-    const int kCols = TmaShape<C>::kCols;
+size_t tma_smem(int S, int nst, int chunk) {
+    const int kCols = chunk / (kTileRows * (int)sizeof(C));
     const int nvec = ((S + kCols - 1) / kCols) * kCols;
-    return (size_t)nst * kChunkBytes + 2 * (size_t)nst * sizeof(uint64_t) + 2 * (size_t)nvec * sizeof(C);
+    return (size_t)nst * chunk + 2 * (size_t)nst * sizeof(uint64_t) + 2 * (size_t)nvec * sizeof(C);
+}
+
+template <typename C>
+void (*sweep_kernel(TmaVariant v))(const SweepTmaParams) {
+    if (v.chunk == 8192)
+        return v.cps == 2 ? k_sweep_tma<C, 2, 8192> : v.cps == 4 ? k_sweep_tma<C, 4, 8192> : k_sweep_tma<C, 3, 8192>;
+    return v.cps == 2 ? k_sweep_tma<C, 2, 16384> : v.cps == 4 ? k_sweep_tma<C, 4, 16384> : k_sweep_tma<C, 3, 16384>;
 }
 
 // Sweep arguments of the plan's factors for `nshift` shifts starting at shift 0; the
@@ -744,14 +752,16 @@ SweepArgs sweep_args(const kore_plan *p, int nshift) {
     return a;
 }
 
-// Tensor maps, ring depth and the cooperative launch of k_sweep_tma with cps CTAs per SM
-// (2, 3 or 4); the completion counters a.cnt are zeroed first.
+// Tensor maps, ring depth and the cooperative launch of the k_sweep_tma variant v (CTAs
+// per SM, chunk bytes); the completion counters a.cnt are zeroed first.
 template <typename C>
-int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st, int cps = kTmaCtasPerSm) {
+int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st, TmaVariant v = kTmaDefault) {
     SweepTmaParams P;
     P.a = a;
     const int rb = (int)sizeof(C) / 2;
-    const int kCols = TmaShape<C>::kCols;
+    const int cps = v.cps;
+    if (v.chunk != 8192 && v.chunk != 16384) return KORE_EINVAL;
+    const int kCols = v.chunk / (kTileRows * (int)sizeof(C));
     const int ns = a.nshift;
     KORE_TRY(kore_encode_block_map(&P.maps[kMapDinv], p->d_Dinv, rb, p->S, p->K, ns, p->f_stride(), kTileRows, kCols));
     KORE_TRY(kore_encode_block_map(&P.maps[kMapG], p->d_Gm, rb, p->S, p->K, ns, p->f_stride(), kTileRows, kCols));
@@ -762,18 +772,17 @@ int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st, int cp
     int smem_sm = 0, smem_blk = 0;
     KORE_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, p->device));
     KORE_CUDA_TRY(cudaDeviceGetAttribute(&smem_blk, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
-    void (*kern)(const SweepTmaParams) = (cps == 2) ? k_sweep_tma<C, 2> : (cps == 4) ? k_sweep_tma<C, 4>
-                                                                                    : k_sweep_tma<C, 3>;
+    void (*kern)(const SweepTmaParams) = sweep_kernel<C>(v);
     cudaFuncAttributes fa;
     KORE_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
     const size_t static_smem = fa.sharedSizeBytes + 1024;   // + the per-CTA reserve of the SM
     const size_t budget = std::min<size_t>((size_t)smem_sm / cps - static_smem,
                                            (size_t)smem_blk - fa.sharedSizeBytes);
     int nst = kMaxRing;
-    while (nst > 2 && tma_smem<C>(p->S, nst) > budget) --nst;
-    if (tma_smem<C>(p->S, nst) > budget) return KORE_EINVAL;
+    while (nst > 2 && tma_smem<C>(p->S, nst, v.chunk) > budget) --nst;
+    if (tma_smem<C>(p->S, nst, v.chunk) > budget) return KORE_EINVAL;
     P.nst = nst;
-    const size_t smem = tma_smem<C>(p->S, nst);
+    const size_t smem = tma_smem<C>(p->S, nst, v.chunk);
     KORE_TRY(kore_allow_max_dyn_smem(kern, p->device));
     int occ = 0;
     KORE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTmaThreads, smem));
@@ -787,7 +796,7 @@ int launch_sweep(const kore_plan *p, const SweepArgs &a, cudaStream_t st, int cp
     return KORE_OK;
 }
 
-// Autotuner of the sweep's CTAs per SM, keyed on the plan's shape: the first
+// Autotuner of the sweep's variant (CTAs per SM, chunk size), keyed on the plan's shape: the first
 // non-accumulating sweep of a shape (padded block size, blocks, width of the level-0
 // coupling rows, precision, shifts) times every variant on its own work (a
 // non-accumulating sweep gives the same result each time it runs) and keeps the fastest
@@ -799,28 +808,28 @@ struct TuneKey {
     }
 };
 std::mutex g_tune_mu;
-std::map<TuneKey, int> g_tune;
+std::map<TuneKey, TmaVariant> g_tune;
 
 template <typename C>
-int tune_sweep(kore_plan *p, const SweepArgs &a, int *best) {
+int tune_sweep(kore_plan *p, const SweepArgs &a, TmaVariant *best) {
     cudaEvent_t e0, e1;
     KORE_CUDA_TRY(cudaEventCreate(&e0));
     KORE_CUDA_TRY(cudaEventCreate(&e1));
     float best_ms = 1e30f;
     int rc = KORE_OK;
-    *best = kTmaCtasPerSm;
-    for (int cps : kTmaVariants) {
+    *best = kTmaDefault;
+    for (const TmaVariant v : kTmaVariants) {
         float ms = 0.f;
         for (int rep = 0; rep < 2 && rc == KORE_OK; ++rep) {   // the second run is timed
             if (cudaEventRecord(e0, p->stream) != cudaSuccess) rc = KORE_ECUDA;
-            if (rc == KORE_OK) rc = launch_sweep<C>(p, a, p->stream, cps);
+            if (rc == KORE_OK) rc = launch_sweep<C>(p, a, p->stream, v);
             if (rc == KORE_OK && cudaEventRecord(e1, p->stream) != cudaSuccess) rc = KORE_ECUDA;
             if (rc == KORE_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = KORE_ECUDA;
             if (rc == KORE_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = KORE_ECUDA;
         }
         if (rc == KORE_EINVAL) { rc = KORE_OK; continue; }   // the variant does not fit this shape
         if (rc != KORE_OK) break;
-        if (ms < best_ms) { best_ms = ms; *best = cps; }
+        if (ms < best_ms) { best_ms = ms; *best = v; }
     }
     // the chosen variant runs last, so the sweep's outputs are its own
     if (rc == KORE_OK) rc = launch_sweep<C>(p, a, p->stream, *best);
@@ -841,24 +850,25 @@ int sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int a
     a.count = &p->d_ir->sweeps; a.count_total = &p->d_ir->sweeps_total;
     const bool fp64 = p->prec == KORE_PREC_FP64;
     const TuneKey key{p->S, p->K, p->ell_w, p->prec, p->nshift};
-    int cps = 0;
+    TmaVariant v{0, 0};
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune.find(key);
-        if (it != g_tune.end()) cps = it->second;
+        if (it != g_tune.end()) v = it->second;
     }
     int s;
-    if (cps == 0 && !accumulate) {
-        s = fp64 ? tune_sweep<double2>(p, a, &cps) : tune_sweep<float2>(p, a, &cps);
+    if (v.cps == 0 && !accumulate) {
+        s = fp64 ? tune_sweep<double2>(p, a, &v) : tune_sweep<float2>(p, a, &v);
         if (s == KORE_OK) {
             std::lock_guard<std::mutex> lk(g_tune_mu);
-            g_tune[key] = cps;
+            g_tune[key] = v;
         }
     } else {
-        if (cps == 0) cps = kTmaCtasPerSm;
-        s = fp64 ? launch_sweep<double2>(p, a, p->stream, cps) : launch_sweep<float2>(p, a, p->stream, cps);
+        if (v.cps == 0) v = kTmaDefault;
+        s = fp64 ? launch_sweep<double2>(p, a, p->stream, v) : launch_sweep<float2>(p, a, p->stream, v);
     }
-    p->sweep_cps = cps;
+    p->sweep_cps = v.cps;
+    p->sweep_chunk = v.chunk;
     if (p->prof) KORE_TRY(kore_prof_mark(p, 0, false));
     return s;
 }
@@ -1181,7 +1191,7 @@ int noalloc_sweep(kore_plan *p, NoAllocScratch *s, const double2 *b, const doubl
     a.f = s->f; a.z = s->z; a.x = s->x;
     a.out = x; a.accumulate = accumulate; a.cnt = s->cnt; a.err = &s->err;
     a.skip = skip; a.skip_stride = 0; a.count = &s->ir.sweeps; a.count_total = &s->ir.sweeps_total;
-    return launch_sweep<C>(p, a, st, p->sweep_cps > 0 ? p->sweep_cps : kTmaCtasPerSm);
+    return launch_sweep<C>(p, a, st, p->sweep_cps > 0 ? TmaVariant{p->sweep_cps, p->sweep_chunk} : kTmaDefault);
 }
 
 int noalloc_solve(kore_plan *p, NoAllocScratch *s, const double2 *b_dev, double2 *x_dev, double tol, cudaStream_t st) {

@@ -151,12 +151,12 @@ class Pencil:
     def profile(self, enable):
         """Start (True) / stop (False) CUDA-event timing of the sweep and factorisation
         kernels; returns the totals recorded so far."""
-        out = np.zeros(13)
+        out = np.zeros(14)
         L.check(self.lib.kore_profile(self._plan, 1 if enable else 0, L.ptr(out)), "kore_profile")
         return {"sweep_ms": out[0], "sweeps": int(out[1]), "factor_ms": out[2], "factors": int(out[3]),
                 "sweep_bytes": out[4], "factor_flops": out[5], "spmv_ms": out[6], "spmv_n": int(out[7]),
                 "ortho_ms": out[8], "ortho_n": int(out[9]), "schur_ms": out[10], "schur_n": int(out[11]),
-                "sweep_ctas_per_sm": int(out[12])}
+                "sweep_ctas_per_sm": int(out[12]), "sweep_chunk_bytes": int(out[13])}
 
     def device_bytes(self):
         v = C.c_int64()
