@@ -224,6 +224,15 @@ int kore_eigs_shifts(kore_plan *plan, int ntarget, const kore_eps_opts *opts, do
 /* y = A x - lambda B x (FP64, original order, host pointers); residual checks. */
 int kore_residual(kore_plan *plan, double lam_re, double lam_im, const double *x, double *y);
 
+/*
+ * Pins the sweep variant for every later sweep of the process: ctas_per_sm 2, 3 or 4
+ * and chunk_bytes 8192 or 16384 (the ring slot size); (0, 0) restores the autotuner,
+ * which otherwise times the six variants on the first sweep of each plan shape and
+ * keeps the fastest.  KORE_EINVAL for any other pair.  For reproducible timings and
+ * for testing each variant.
+ */
+int kore_sweep_variant(int ctas_per_sm, int chunk_bytes);
+
 /* The CUDA stream (cudaStream_t) every kernel of the plan is launched on. */
 int kore_plan_stream(const kore_plan *plan, void **stream);
 

@@ -33,7 +33,7 @@ def default_ncv(n, nev):
 EXPORTS = ("kore_plan_create", "kore_factor", "kore_factor_shifts", "kore_solve", "kore_solve_dev",
            "kore_solve_dev_noalloc", "kore_eigs", "kore_eigs_shifts", "kore_residual", "kore_plan_stream", "kore_profile",
            "kore_plan_bytes", "kore_plan_estimate_bytes", "kore_batch_create", "kore_batch_submit",
-           "kore_batch_poll", "kore_batch_stats", "kore_batch_destroy", "kore_tc_selftest", "kore_gegenbauer_mult", "kore_flow_diagnostics", "kore_assemble_blocks", "kore_kernel_launches",
+           "kore_batch_poll", "kore_batch_stats", "kore_batch_destroy", "kore_tc_selftest", "kore_gegenbauer_mult", "kore_flow_diagnostics", "kore_assemble_blocks", "kore_sweep_variant", "kore_kernel_launches",
            "kore_status_string", "kore_plan_destroy")
 
 
@@ -159,6 +159,7 @@ def _bind(lib):
     lib.kore_tc_selftest.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
     lib.kore_gegenbauer_mult.argtypes = [C.c_int, C.c_int, P, C.c_double, C.c_int, P]
     lib.kore_flow_diagnostics.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, P, C.c_int, P, P, C.c_int, P]
+    lib.kore_sweep_variant.argtypes = [C.c_int, C.c_int]
     lib.kore_assemble_blocks.argtypes = [C.c_int, C.c_int, C.c_int, P, C.c_int64, P, C.c_int, P, C.c_int64, P, P, P,
                                          P, P, P, P, C.c_int64, P, P, C.c_int64, P, P]
     for name in EXPORTS:

@@ -809,6 +809,7 @@ struct TuneKey {
 };
 std::mutex g_tune_mu;
 std::map<TuneKey, TmaVariant> g_tune;
+TmaVariant g_force{0, 0};   // kore_sweep_variant: every sweep uses it instead of the autotuner's choice
 
 template <typename C>
 int tune_sweep(kore_plan *p, const SweepArgs &a, TmaVariant *best) {
@@ -851,13 +852,15 @@ int sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int a
     const bool fp64 = p->prec == KORE_PREC_FP64;
     const TuneKey key{p->S, p->K, p->ell_w, p->prec, p->nshift};
     TmaVariant v{0, 0};
+    bool forced = false;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune.find(key);
-        if (it != g_tune.end()) v = it->second;
+        if (g_force.cps != 0) { v = g_force; forced = true; }
+        else if (it != g_tune.end()) v = it->second;
     }
     int s;
-    if (v.cps == 0 && !accumulate) {
+    if (v.cps == 0 && !accumulate && !forced) {
         s = fp64 ? tune_sweep<double2>(p, a, &v) : tune_sweep<float2>(p, a, &v);
         if (s == KORE_OK) {
             std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -872,6 +875,19 @@ int sweep(kore_plan *p, const double2 *b, const double *bnorm, double2 *x, int a
     if (p->prof) KORE_TRY(kore_prof_mark(p, 0, false));
     return s;
 }
+
+}  // namespace
+
+extern "C" int kore_sweep_variant(int ctas_per_sm, int chunk_bytes) {
+    bool ok = ctas_per_sm == 0 && chunk_bytes == 0;
+    for (const TmaVariant v : kTmaVariants) ok = ok || (v.cps == ctas_per_sm && v.chunk == chunk_bytes);
+    if (!ok) return KORE_EINVAL;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_force = TmaVariant{ctas_per_sm, chunk_bytes};
+    return KORE_OK;
+}
+
+namespace {
 
 unsigned absmax_grid(int64_t np) { return std::min<unsigned>(kore_div_up(np, 256), 1024u); }
 

@@ -185,6 +185,12 @@ def kernel_launches():
     return int(L.load().kore_kernel_launches())
 
 
+def sweep_variant(ctas_per_sm=0, chunk_bytes=0):
+    """Pin the sweep variant for every later sweep of the process (2, 3 or 4 CTAs per SM;
+    8192 or 16384-byte ring slots); sweep_variant() returns to the autotuner's choice."""
+    L.check(L.load().kore_sweep_variant(int(ctas_per_sm), int(chunk_bytes)), "kore_sweep_variant")
+
+
 def forced_sweep(pencil, omegas, b, precision="mixed", group=16, refine_tol=0.0, scale=1.0):
     """Forced solves over a frequency sweep on one eigen pencil.
 
