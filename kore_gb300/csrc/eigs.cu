@@ -430,7 +430,26 @@ __global__ void __launch_bounds__(kDotThreads) k_mdot(int64_t np, TVec V, TVec w
         double2 acc[kDotChunk];
 #pragma unroll
         for (int t = 0; t < kDotChunk; ++t) acc[t] = mk(0.0, 0.0);
-        for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < np; r += (int64_t)gridDim.x * blockDim.x) {
+        // two rows per step, both rows' loads issued before their products: the CTA's
+        // warps meet at every chunk's reduction, so a row's load latency is not hidden by
+        // other warps' products
+        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+        int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+        for (; r + stride < np; r += 2 * stride) {
+            const int64_t r2 = r + stride;
+            const double2 wa = wt[r], wb = wt[r2];
+            double2 va[kDotChunk], vb[kDotChunk];
+#pragma unroll
+            for (int t = 0; t < kDotChunk; ++t) {
+                const bool col = c0 + t < ncol;
+                va[t] = col ? Vt[r + (int64_t)(c0 + t) * np] : wa;
+                vb[t] = col ? Vt[r2 + (int64_t)(c0 + t) * np] : wb;
+            }
+#pragma unroll
+            for (int t = 0; t < kDotChunk; ++t)
+                if (c0 + t < nc) acc[t] = cfmaconj(cfmaconj(acc[t], va[t], wa), vb[t], wb);
+        }
+        if (r < np) {
             const double2 wr = wt[r];
 #pragma unroll
             for (int t = 0; t < kDotChunk; ++t)
