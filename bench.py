@@ -43,7 +43,7 @@ WORKLOADS = {
 # frequencies uniform in [-2, 2] solved `group` at a time, then `instances` uneven
 # problems (m, N, lmax, Ek drawn from the sweep's ranges) solved concurrently.
 FORCED = {
-    "forced4": dict(m=2, symm=1, Ek=1e-6, N=240, lmax=301, ricb=0.35, nfreq=512, group=16, instances=16),
+    "forced4": dict(m=2, symm=1, Ek=1e-6, N=240, lmax=301, ricb=0.35, nfreq=512, group=16, instances=256),
     # small version of the same for quick checks
     "forced4s": dict(m=2, symm=1, Ek=1e-5, N=96, lmax=61, ricb=0.35, nfreq=64, group=16, instances=4),
 }
@@ -431,28 +431,40 @@ def forced_bench(args, local, c=None, emit=True):
     n = int(Ae.shape[0])
     p.close()
 
-    # uneven instances, four plans in flight at once (each plan has its own stream)
+    # uneven instances, four plans in flight at once (each plan has its own stream); the
+    # pencils are assembled on the GPU 16 at a time, outside the timed region
     inst = uneven_instances(c["instances"])
-    built = []
-    for d in inst:
-        A_i, B_i, nrm_i = hydro_pencil(d["m"], 1, d["Ek"], d["N"], d["lmax"], d["ricb"], with_norm=True)
+
+    def assemble(d):
+        A_i, B_i, nrm_i = hydro_pencil(d["m"], 1, d["Ek"], d["N"], d["lmax"], d["ricb"], with_norm=True,
+                                       assemble_on_device=True, device=local)
         b_i = forcing_vector(d["m"], 1, d["N"], d["lmax"], d["ricb"], 10).toarray().ravel()
-        built.append((d, A_i, B_i, nrm_i, b_i))
+        return d, A_i, B_i, nrm_i, b_i
 
     def one(item):
         d, A_i, B_i, nrm_i, b_i = item
         q = Pencil(A_i, B_i, layout=layout_from_params(hydro_params(d["m"], 1, d["Ek"], d["N"], d["lmax"], d["ricb"])),
                    device=local)
+        info = {}
         with q:
-            x, _ = forced_sweep(q, [d["w"]], b_i, "mixed", 1, refine_tol=1e-14, scale=nrm_i)
+            x, _ = forced_sweep(q, [d["w"]], b_i, "mixed", 1, refine_tol=1e-14, scale=nrm_i, info=info)
         M = (A_i - (1j * d["w"]) * B_i).tocsr()
         r = M @ x[:, 0] - b_i / nrm_i
-        return np.abs(r).max() / (abs(M).sum(axis=1).max() * np.abs(x).max() + np.abs(b_i / nrm_i).max())
+        return (np.abs(r).max() / (abs(M).sum(axis=1).max() * np.abs(x).max() + np.abs(b_i / nrm_i).max()),
+                info["escalated"], info["mixed_resid_max"], d)
 
-    t0 = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=4) as ex:
-        res_i = list(ex.map(one, built))
-    wall_i = time.perf_counter() - t0
+    res_i, wall_i = [], 0.0
+    for k0 in range(0, len(inst), 16):
+        built = [assemble(d) for d in inst[k0:k0 + 16]]
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=4) as ex:
+            res_i += list(ex.map(one, built))
+        wall_i += time.perf_counter() - t0
+        del built
+    ns_i = [(d["lmax"] - d["m"] + 1) * d["N"] for d in inst]
+    worst = sorted(res_i, key=lambda r: -r[2])[:3]
+    esc = sum(r[1] for r in res_i)
+    res_i = [r[0] for r in res_i]
     value = len(om) / wall
     hbytes = (len(om) * n * 16, len(om) * n * 16)
     line = {
@@ -469,8 +481,13 @@ def forced_bench(args, local, c=None, emit=True):
                  "max_rel_diff_mixed_vs_fp64": float(diff)},
         "speedup_vs_fp64": value / (nb64 * G / wall64),
         "uneven": {"instances": len(inst), "value": len(inst) / wall_i, "unit": "solves/s (plan + factor + solve, "
-                   "4 plans in flight)", "max_resid": float(max(res_i)),
-                   "sizes": [[d["m"], d["N"], d["lmax"], float(f"{d['Ek']:.3g}")] for d in inst]},
+                   "4 plans in flight, 16 instances per round)", "max_resid": float(max(res_i)),
+                   "unknowns": {"min": min(ns_i), "max": max(ns_i), "mean": float(np.mean(ns_i))},
+                   "escalated_to_fp64": int(esc),
+                   "worst_mixed_refinement": [{"m": d["m"], "N": d["N"], "lmax": d["lmax"], "Ek": float(f"{d['Ek']:.3g}"),
+                                               "w": float(f"{d['w']:.4g}"), "mixed_eta": float(e)}
+                                              for _, _, e, d in worst],
+                   "first_sizes_m_N_lmax_Ek": [[d["m"], d["N"], d["lmax"], float(f"{d['Ek']:.3g}")] for d in inst[:8]]},
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": hbytes[0] // len(gt),

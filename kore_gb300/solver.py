@@ -191,7 +191,8 @@ def sweep_variant(ctas_per_sm=0, chunk_bytes=0):
     L.check(L.load().kore_sweep_variant(int(ctas_per_sm), int(chunk_bytes)), "kore_sweep_variant")
 
 
-def forced_sweep(pencil, omegas, b, precision="mixed", group=16, refine_tol=0.0, scale=1.0):
+def forced_sweep(pencil, omegas, b, precision="mixed", group=16, refine_tol=0.0, scale=1.0, escalate_tol=1e-10,
+                 info=None):
     """Forced solves over a frequency sweep on one eigen pencil.
 
     kore's forced matrix at forcing frequency w is ||B||_F (A_eig - i w B_eig)
@@ -199,21 +200,36 @@ def forced_sweep(pencil, omegas, b, precision="mixed", group=16, refine_tol=0.0,
     shifted solve x_w = (A_eig - i w B_eig)^-1 b_w / scale with scale = ||B||_F.  The
     frequencies are factorised and solved ``group`` at a time in batched kernels.
 
+    Mixed precision: when the FP64 refinement of a group stops above ``escalate_tol``
+    (normwise backward error; the complex64 factors of a badly conditioned shift do not
+    contract the error), that group is factorised again in FP64 and solved with those
+    factors, so every returned solve meets the bound the direct FP64 solve meets.
+
     b: (n,) right-hand side shared by every frequency, or (n, F) one per frequency.
-    Returns (X (n, F), per-group wall seconds).
+    Returns (X (n, F), per-group wall seconds); ``info`` (a dict) receives the number of
+    escalated frequencies and the largest backward error the mixed refinement reached.
     """
     om = np.asarray(omegas, dtype=np.float64).ravel()
     F = len(om)
     b = np.asarray(b)
     X = np.empty((pencil.n, F), dtype=np.complex128)
     times = []
+    escalated, resid = 0, 0.0
     for g0 in range(0, F, group):
         sl = slice(g0, min(F, g0 + group))
         t = time.perf_counter()
         pencil.factor_shifts(1j * om[sl], precision)
         rhs = (b[:, sl] if b.ndim == 2 else np.repeat(b.reshape(-1, 1), sl.stop - sl.start, axis=1)) / scale
-        X[:, sl] = pencil.solve(rhs, refine_tol=refine_tol)
+        X[:, sl], st = pencil.solve(rhs, refine_tol=refine_tol, stats=True)
+        if precision == "mixed":
+            resid = max(resid, st["solve_resid_max"])
+            if escalate_tol and not st["solve_resid_max"] <= escalate_tol:
+                pencil.factor_shifts(1j * om[sl], "fp64")
+                X[:, sl] = pencil.solve(rhs)
+                escalated += sl.stop - sl.start
         times.append(time.perf_counter() - t)
+    if info is not None:
+        info.update(escalated=escalated, mixed_resid_max=resid)
     return X, times
 
 
@@ -439,6 +455,7 @@ class KSP:
         self.rtol, self.max_it = 1e-8, 10000
         self.precision = "fp64"
         self.refine_tol = 0.0
+        self.escalate_tol = 1e-10   # mixed: refactorise in FP64 when the refinement stops above it
         self.stats = {}
 
     def create(self, comm=None):
@@ -469,6 +486,11 @@ class KSP:
         if p.sigma != 0j or p.precision != self.precision:
             p.factor(0.0, self.precision)
         sol, st = p.solve(b, refine_tol=self.refine_tol, stats=True)
+        st["escalated"] = 0
+        if self.precision == "mixed" and self.escalate_tol and not st["solve_resid_max"] <= self.escalate_tol:
+            p.factor(0.0, "fp64")
+            sol = p.solve(b)
+            st["escalated"] = 1
         self.stats = st
         if x is not None:
             x[...] = sol
