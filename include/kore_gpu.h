@@ -130,6 +130,8 @@ typedef struct {
     int32_t factor_reused;     /* eigen: the slot already held the factors of the shift used */
     int32_t warm_started;      /* eigen: started from the slot's last eigenvectors (opts.warm) */
     double  shift_re, shift_im;   /* eigen: the shift of the spectral transformation used */
+    int32_t escalated;         /* served forced request: solved again with FP64 factors because the
+                                  mixed refinement stopped above 1e-10 */
 } kore_stats;
 
 /* Replaces bin/solve.py:40-86 (load_csr + PETSc Mat assembly of A and B). */

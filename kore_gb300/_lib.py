@@ -98,6 +98,7 @@ class Stats(C.Structure):
         ("warm_started", C.c_int32),
         ("shift_re", C.c_double),
         ("shift_im", C.c_double),
+        ("escalated", C.c_int32),
     ]
 
     def as_dict(self):

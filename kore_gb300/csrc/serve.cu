@@ -21,6 +21,9 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// backward error above which a mixed-precision forced solve is redone with FP64 factors
+constexpr double kForcedEscalateTol = 1e-10;
+
 double ms_since(Clock::time_point a, Clock::time_point b) {
     return std::chrono::duration<double, std::milli>(b - a).count();
 }
@@ -301,7 +304,21 @@ int run_request(kore_batch *b, Request *q, CachedPlan *c) {
     std::vector<double> rhs(r.rhs, r.rhs + 2 * n);
     if (sc != 1.0)
         for (double &v : rhs) v *= sc;
-    return kore_solve(c->plan, rhs.data(), r.x, 1, r.refine_tol, nullptr);
+    kore_stats st{};
+    int rc = kore_solve(c->plan, rhs.data(), r.x, 1, r.refine_tol, &st);
+    // mixed precision: a refinement that stopped above the forced solve's bound (the
+    // complex64 factors of a badly conditioned shift do not contract the error) is
+    // redone with FP64 factors, which the cache then holds for this shift
+    if (rc == KORE_OK && r.precision == KORE_PREC_MIXED && !(st.solve_resid_max <= kForcedEscalateTol)) {
+        c->factored = false;
+        KORE_TRY(kore_factor(c->plan, r.sigma_re, r.sigma_im, KORE_PREC_FP64));
+        c->factored = true;
+        c->prec = KORE_PREC_FP64;
+        rc = kore_solve(c->plan, rhs.data(), r.x, 1, 0.0, &st);
+        st.escalated = 1;
+    }
+    if (r.stats) *r.stats = st;
+    return rc;
 }
 
 void worker(kore_batch *b) {

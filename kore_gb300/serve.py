@@ -96,7 +96,9 @@ class Server:
                                       "timing": timing, "target": target, "stats_struct": st})
 
     def submit_forced(self, data, sigma, rhs, scale=1.0, precision="mixed", refine_tol=0.0, key=None):
-        """x = (A - sigma B)^-1 rhs / scale (kore_solve); returns a ticket."""
+        """x = (A - sigma B)^-1 rhs / scale (kore_solve); returns a ticket.  In mixed
+        precision a solve whose refinement stops above a backward error of 1e-10 is redone
+        with FP64 factors (result["stats"]["escalated"])."""
         sigma = complex(sigma)
         b = np.ascontiguousarray(np.asarray(rhs, dtype=np.complex128).ravel())
         if b.size != data.n:
@@ -114,8 +116,11 @@ class Server:
         r.refine_tol = float(refine_tol)
         r.x = x.ctypes.data
         r.timing_ms = timing.ctypes.data
-        keep = (data, b, x, timing)
-        return self._submit(r, keep, {"kind": "forced", "x": x, "timing": timing, "sigma": sigma})
+        st = L.Stats()
+        r.stats = C.addressof(st)
+        keep = (data, b, x, timing, st)
+        return self._submit(r, keep, {"kind": "forced", "x": x, "timing": timing, "sigma": sigma,
+                                      "stats_struct": st})
 
     def poll(self, ticket, wait_ms=0):
         """None while the request runs, else its result (see :meth:`result`)."""
@@ -130,11 +135,10 @@ class Server:
         out["status"] = st.value
         t = res["timing"]
         out["queued_ms"], out["run_ms"], out["total_ms"] = float(t[0]), float(t[1]), float(t[2])
+        out["stats"] = out.pop("stats_struct").as_dict()
         if res["kind"] == "eigen":
             k = res["nconv"].value
             out["nconv"] = k
-            st = out.pop("stats_struct")
-            out["stats"] = st.as_dict()
             out["evals"] = res["evals"][:k]
             if res["evecs"] is not None:
                 out["evecs"] = res["evecs"][:k].T

@@ -114,3 +114,33 @@ def test_eigen_requests_join_a_running_engine(gpu_lib, case):
         assert np.array_equal(alone["evecs"], r["evecs"])
         ref, _ = shift_invert_eigs(A, B, t, 6, "TM")
         assert match_eigs(r["evals"][:6], ref).max() < 1e-10
+
+
+def test_served_forced_request_escalates_when_refinement_stalls(gpu_lib):
+    """A served mixed-precision forced request on the badly conditioned uneven instance
+    of the forcing sweep (m=1, N=80, lmax=248, Ek=1.67e-7): the result meets 1e-12, with
+    FP64 factors when the complex64 refinement stopped above 1e-10; a well-conditioned
+    request is not escalated."""
+    from kore_gb300.assembly import forcing_vector, hydro_params, hydro_pencil
+    from kore_gb300.serve import PencilData, Server
+    from kore_gb300.structure import layout_from_params
+    m, N, lmax, Ek, w = 1, 80, 248, 1.67e-7, 0.3729
+    A, B, nrm = hydro_pencil(m, 1, Ek, N, lmax, 0.35, with_norm=True)
+    b = forcing_vector(m, 1, N, lmax, 0.35, 10).toarray().ravel()
+    P = PencilData(A, B, layout=layout_from_params(hydro_params(m, 1, Ek, N, lmax, 0.35)))
+    with Server(workers=1) as srv:
+        r = srv.result(srv.submit_forced(P, 1j * w, b, scale=nrm, refine_tol=1e-14))
+    st = r["stats"]
+    assert solve_residual((A - 1j * w * B).tocsr(), r["x"], b / nrm) < 1e-12, st
+    assert st["escalated"] == 1 or st["solve_resid_max"] <= 1e-10, st
+
+
+def test_served_forced_request_not_escalated(gpu_lib, case):
+    from kore_gb300.serve import Server
+    meta, A, B, P = data_of(case, "shell_m2_ek1e-4")
+    rng = np.random.default_rng(2)
+    b = rng.standard_normal(P.n) + 1j * rng.standard_normal(P.n)
+    with Server(workers=1) as srv:
+        r = srv.result(srv.submit_forced(P, 0.4j, b, refine_tol=1e-14))
+    assert r["stats"]["escalated"] == 0 and r["stats"]["solve_resid_max"] <= 1e-10, r["stats"]
+    assert solve_residual((A - 0.4j * B).tocsr(), r["x"], b) < 1e-13
