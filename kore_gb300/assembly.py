@@ -27,6 +27,7 @@ band at once.
 """
 import contextlib
 import math
+import threading
 
 import numpy as np
 import scipy.fft as sfft
@@ -288,18 +289,23 @@ def boundary_values(x, N, nder, ricb, rcmb=RCMB):
 
 
 # Inside ``lazy_blocks()`` kron_sum and bc_block return LazyBlock term lists instead of
-# sparse matrices, for assemble_grid to assemble on the GPU (one thread at a time).
-_LAZY = [False]
+# sparse matrices, for assemble_grid to assemble on the GPU (per thread).
+_LAZY_STATE = threading.local()
+
+
+def _lazy():
+    return getattr(_LAZY_STATE, "on", False)
 
 
 @contextlib.contextmanager
 def lazy_blocks():
     """Build the blocks of the pencil as term lists (LazyBlock) for ``assemble_grid``."""
-    _LAZY[0] = True
+    prev = _lazy()
+    _LAZY_STATE.on = True
     try:
         yield
     finally:
-        _LAZY[0] = False
+        _LAZY_STATE.on = prev
 
 
 class LazyBlock:
@@ -344,14 +350,14 @@ def kron_sum(lrow, lcol, terms):
     lrow = np.asarray(lrow)
     lcol = np.asarray(lcol)
     pos = {int(l): j for j, l in enumerate(lcol)}
-    out = LazyBlock(lrow.size, lcol.size) if _LAZY[0] else None
+    out = LazyBlock(lrow.size, lcol.size) if _lazy() else None
     for d, coef, M in terms:
         ks = np.array([k for k, l in enumerate(lrow) if int(l) + d in pos], dtype=np.int64)
         if ks.size == 0:
             continue
         js = np.array([pos[int(lrow[k]) + d] for k in ks], dtype=np.int64)
         vals = np.asarray(coef(lrow[ks].astype(float)), dtype=complex) * np.ones(ks.size)
-        if _LAZY[0]:
+        if _lazy():
             out.terms.append((ks, js, vals, M))
             continue
         P = ss.csr_matrix((vals, (ks, js)), shape=(lrow.size, lcol.size))
@@ -367,8 +373,10 @@ def grid_arrays(grid, n1):
     patterns of the distinct block signatures (the (block offset, operator) pairs and
     boundary rows of a row block) and the CSR row pointer."""
     nsec_r, nsec_c = len(grid), len(grid[0])
-    nrow_sec = [next(c.nrow for c in row if c is not None) for row in grid]
-    ncol_sec = [next(grid[a][b].ncol for a in range(nsec_r) if grid[a][b] is not None) for b in range(nsec_c)]
+    nrow_sec = [next((c.nrow for c in row if c is not None), None) for row in grid]
+    ncol_sec = [next((grid[a][b].ncol for a in range(nsec_r) if grid[a][b] is not None), None) for b in range(nsec_c)]
+    if None in nrow_sec or None in ncol_sec:
+        raise ValueError("every section row and column of the grid needs at least one block")
     ro = np.concatenate([[0], np.cumsum(nrow_sec)])
     co = np.concatenate([[0], np.cumsum(ncol_sec)])
     nblk = int(ro[-1])
@@ -524,7 +532,7 @@ def bc_block(rows_list, nrow, N1):
     """Block-diagonal matrix holding, for each l-block k, the boundary rows rows_list[k]
     (nrow rows of N1 Chebyshev coefficients) in its first nrow rows (a LazyBlock inside
     ``lazy_blocks()``)."""
-    if _LAZY[0]:
+    if _lazy():
         return LazyBlock(len(rows_list), len(rows_list), bc=(nrow, np.stack([np.asarray(r)[:nrow] for r in rows_list])))
     data, ri, ci = [], [], []
     for k, rows in enumerate(rows_list):

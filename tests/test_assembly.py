@@ -203,3 +203,22 @@ def test_mac_device_assembly_inputs_rebuild_host_pencil():
     B = ss.csr_matrix(_emulate_assemble_kernel(asm.grid_arrays(Bg, N)).real)
     assert ssl.norm(A0 - A0h) <= 1e-14 * ssl.norm(A0h)
     assert ssl.norm(B - Bh) <= 1e-14 * ssl.norm(Bh)
+
+
+def test_lazy_blocks_are_per_thread_and_grid_checks():
+    import threading
+    from kore_gb300 import assembly as asm
+    seen = {}
+
+    def other():
+        seen["other"] = asm.kron_sum([2, 3], [2, 3], [(0, lambda l: l, np.eye(4))])
+
+    with asm.lazy_blocks():
+        mine = asm.kron_sum([2, 3], [2, 3], [(0, lambda l: l, np.eye(4))])
+        t = threading.Thread(target=other)
+        t.start()
+        t.join()
+    assert isinstance(mine, asm.LazyBlock) and not isinstance(seen["other"], asm.LazyBlock)
+    assert not isinstance(asm.kron_sum([2], [2], [(0, lambda l: l, np.eye(2))]), asm.LazyBlock)
+    with pytest.raises(ValueError):
+        asm.grid_arrays([[mine, None], [None, None]], 4)
