@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 from conftest import ROOT
 
 
@@ -87,3 +89,35 @@ def test_default_basis_size_rule():
     assert default_ncv(240000, 4) == 19       # SLEPc's nev + 15 dominates
     assert default_ncv(240000, 40) == 80      # SLEPc's 2 nev above the cap (refused by the engine)
     assert default_ncv(30, 16) == 30          # never above n
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Sizes and field offsets of the ctypes mirrors in kore_gb300._lib against the C
+    structs of include/kore_gpu.h, compiled with the host compiler."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from kore_gb300 import _lib as L
+    pairs = [("kore_pencil_desc", L.PencilDesc), ("kore_eps_opts", L.EpsOpts), ("kore_stats", L.Stats),
+             ("kore_request", L.Request)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "kore_gpu.h"', "int main(void) {"]
+    for cname, cls in pairs:
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = {}
+    for row in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        name, field, val = row.split()
+        got[(name, field)] = int(val)
+    for cname, cls in pairs:
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
