@@ -443,11 +443,16 @@ def grid_arrays(grid, n1):
             ii.append(np.repeat(np.arange(g), n1)); dd.append(np.zeros(g * n1, dtype=np.int64))
             jj.append(np.tile(np.arange(n1), g))
         ii, dd, jj = (np.concatenate(x).astype(np.int64) for x in (ii, dd, jj))
-        u = np.unique(np.stack([ii, dd, jj], axis=1), axis=0)   # sorted by row, then (dC, j)
-        rowlen[s] = np.bincount(u[:, 0], minlength=n1)
+        # one integer key per (row, block offset, column), ordered as those triples
+        span = 2 * nblk + 1
+        key = np.unique((ii * span + (dd + nblk)) * n1 + jj)   # sorted by row, then (dC, j)
+        u_j = key % n1
+        u_d = (key // n1) % span - nblk
+        u_i = key // (n1 * span)
+        rowlen[s] = np.bincount(u_i, minlength=n1)
         sig_rowptr[s] = base + np.concatenate([[0], np.cumsum(rowlen[s])])
-        pats.append(u[:, 1:].astype(np.int32))
-        base += len(u)
+        pats.append(np.stack([u_d, u_j], axis=1).astype(np.int32))
+        base += len(key)
     sig_pat = np.ascontiguousarray(np.concatenate(pats)) if pats else np.zeros((0, 2), np.int32)
     indptr = np.concatenate([[0], np.cumsum(rowlen[sig_of].ravel())]).astype(np.int64)
     nnz = int(indptr[-1])
