@@ -211,6 +211,20 @@ METRIC = "eigenpairs/s (shift-invert Krylov-Schur, nev converged, resid<=1e-10)"
 REFERENCE_BUDGET_S = 600.0
 
 
+def replica_aggregate(dist, total_ms, units, device):
+    """Whole-job figures of N independent replicas (one per GPU, no data-path
+    collective): the slowest replica's time (max over ranks) and the units every rank
+    processed (sum).  With dist None (one process) the rank's own figures."""
+    if dist is None:
+        return total_ms, units
+    import torch
+    t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(round(u.item()))
+
+
 def reference_arm(args, rank, world):
     """The reference's CPU solve path restated by the oracle (SuperLU factorisation of
     A - tau B + ARPACK shift-invert, SLEPc's `which` ordering), timed on the host cores on
@@ -802,13 +816,7 @@ def main():
     prof = p.profile(False)
     launches = kernel_launches() - launches0
     total_ms = t0.elapsed_time(t1)
-    if dist:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
-        pp = torch.tensor([float(pairs)], device="cuda")
-        dist.all_reduce(pp, op=dist.ReduceOp.SUM)
-        pairs = int(pp.item())
+    total_ms, pairs = replica_aggregate(dist, total_ms, pairs, "cuda")
     value = pairs / (total_ms / 1e3)
     lam, X = E.eigenvalues(), E.eigenvectors()
     res = rel_residuals(A, B, lam[:nev], X[:, :nev])
