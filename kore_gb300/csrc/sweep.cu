@@ -124,9 +124,10 @@ constexpr int kTmaThreads = kTmaConsumers + 64;   // + one producer warp + one d
 constexpr int kTileRows = 32;
 constexpr int kMaxRing = 24;
 constexpr int kEllReg = 4;   // level-0 coupling entries per thread held in registers (width 32)
-// input-vector loads in flight per consumer lane: a two-matrix tile's slice (2 x 7 x 16
-// entries per warp at S = 400) takes one round of L2 latency with 8, two with 4; the
-// variants whose register budget (65536 / (192 CPS)) cannot hold 8 keep 4
+// input-vector loads in flight per consumer lane: a two-matrix tile's slice (about 2 S / 4
+// entries per warp: 2 x 7 x 16 at S = 400 with 16 KB chunks, 2 x 13 x 8 with 8 KB) takes
+// one round of L2 latency with 8, two with 4; the variants whose register budget
+// (65536 / (192 CPS)) cannot hold 8 keep 4
 template <typename C, int CPS> constexpr int fill_of() { return (CPS == 2 || (CPS == 3 && sizeof(C) == 8)) ? 8 : 4; }
 
 enum { kMapDinv = 0, kMapG = 1, kMapH = 2, kMapLU = 3 };
