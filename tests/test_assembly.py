@@ -222,3 +222,37 @@ def test_lazy_blocks_are_per_thread_and_grid_checks():
     assert not isinstance(asm.kron_sum([2], [2], [(0, lambda l: l, np.eye(2))]), asm.LazyBlock)
     with pytest.raises(ValueError):
         asm.grid_arrays([[mine, None], [None, None]], 4)
+
+
+def test_device_assembly_pattern_covers_fullsize_pencil():
+    """At the 240,000-unknown bench size (too large for the kernel's numpy restatement):
+    the row patterns that grid_arrays gives the GPU kernel hold every stored entry of the
+    host assembly, A and B, so the kernel writes every value somewhere."""
+    import scipy.sparse as ss
+    from kore_gb300 import assembly as asm
+    m, symm, Ek, N, lmax, ricb = 2, 1, 1e-7, 400, 601, 0.35
+    lp, lt = asm.ell(m, lmax, symm)
+    R = asm.RadialOperators(N, ricb)
+    with asm.lazy_blocks():
+        App, Apt, Atp, Att, Up, Ut = asm.momentum_blocks(R.op, m, lp, lt, Ek, 0.0)
+        BCp, BCt = asm.velocity_bc_blocks(lp, lt, N, ricb)
+    Ah, Bh = asm.hydro_pencil(m, symm, Ek, N, lmax, ricb)
+    for grid, H in (([[App + BCp, Apt], [Atp, Att + BCt]], Ah), ([[-Up, None], [None, -Ut]], Bh)):
+        g = asm.grid_arrays(grid, N)
+        n = g["nblk"] * N
+        rows = np.repeat(np.arange(n), np.diff(g["indptr"]))
+        R_of = rows // N
+        i_of = rows % N
+        # the kernel's column of each output slot: (R + dC) N + j from the signature pattern
+        sig = g["sig_of"][R_of]
+        start = g["sig_rowptr"][sig, i_of]
+        k = np.arange(g["nnz"]) - g["indptr"][rows]
+        pat = g["sig_pat"][start + k]
+        cols = (R_of + pat[:, 0]) * N + pat[:, 1]
+        P = ss.csr_matrix((np.ones(g["nnz"]), (rows, cols)), shape=(n, n))
+        assert P.max() == 1                                  # no column twice in a row
+        Hp = H.copy()
+        Hp.data[:] = 1.0
+        assert (Hp - Hp.multiply(P)).nnz == 0                # host entries all in the pattern
+        same_row = rows[1:] == rows[:-1]
+        assert np.all(np.diff(cols)[same_row] > 0)          # columns increase along each row
